@@ -1,0 +1,149 @@
+// args.cuh -- kernel argument blocks and launcher entry points (host view).
+#pragma once
+#include "common.cuh"
+
+namespace pg {
+
+template <class T> __host__ __device__ __forceinline__ T from_bits(uint64_t b) {
+  T t;
+  memcpy(&t, &b, sizeof(T));
+  return t;
+}
+
+// ------------------------------------------------------------ reductions
+enum RedOp {
+  R_SUM = 0, R_DSUM, R_PROD, R_DPROD, R_AVG, R_DAVG, R_MIN, R_MAX,
+  R_MIN_IND, R_MAX_IND, R_NOPS
+};
+
+struct RedArgs {
+  const char *a;      // element (0) of a (already offset)
+  char *b;            // element (0) of b
+  int64_t n;          // reduced length
+  int64_t inc_n;      // a's increment along n (elements)
+  int64_t rows;       // broadcast iterations
+  Loop L;             // pdl 0 = a, pdl 1 = b
+  int bad;            // trans bvalflag
+  uint64_t abad_bits, bbad_bits;  // badvalues (raw bits, in a's / b's type)
+  int abad_isnan, bbad_isnan;
+  int *setbad;        // device flag: PDLSTATESETBAD(output)
+  void *partials;     // split mode: per (row, split) accumulators
+  int64_t *pcounts;   // split mode: per (row, split) good counts
+  int nsplit;         // splits per row (1 = none)
+  int group;          // threads per row (row kernel)
+  int f32_comp;       // compensated float32 sums
+};
+
+struct RedLaunch {
+  int kind;  // 0 rows, 1 thread
+  int grid, block;
+};
+
+pdlgb300_error launch_red_sum(int op, int in_dt, RedArgs args, const RedLaunch &lc,
+                              cudaStream_t s);
+pdlgb300_error launch_red_prod(int op, int in_dt, RedArgs args, const RedLaunch &lc,
+                               cudaStream_t s);
+pdlgb300_error launch_red_minmax(int op, int in_dt, RedArgs args, const RedLaunch &lc,
+                                 cudaStream_t s);
+size_t red_acc_size(int op, int in_dt, int f32_comp);
+
+// ------------------------------------------------------------ plus/mult
+struct BiopArgs {
+  const char *a, *b;
+  char *c;
+  Loop L;  // pdl 0 a, 1 b, 2 c
+  int bad, statebad_a, statebad_b;
+  uint64_t abad, bbad, cbad;
+  int abad_isnan, bbad_isnan;
+  int *setbad;
+};
+pdlgb300_error launch_biop(int op, int dt, const BiopArgs &g, cudaStream_t s);
+
+struct ConvArgs {
+  const char *src;
+  char *dst;
+  Loop L;  // pdl 0 src, 1 dst
+  int bad;
+  uint64_t sbad, dbad;
+  int sbad_isnan;
+};
+pdlgb300_error launch_convert(int from, int to, const ConvArgs &g, cudaStream_t s);
+
+// ----------------------------------------------------------- cumusumover
+struct ScanArgs {
+  const char *a;
+  char *b;
+  int64_t n, inc_a, inc_b, rows;
+  Loop L;  // pdl 0 a, 1 b
+  int bad;
+  uint64_t abad, bbad;
+  int abad_isnan;
+  int f32_comp;
+  int nchunk;        // chunks per row (> 1: three-pass long-row scan)
+  int64_t chunk;     // elements per chunk
+  void *partials;    // per (row, chunk) totals, then exclusive carries
+  int mode;          // 0 full row, 1 chunk totals only, 2 chunk scan with carry
+};
+pdlgb300_error launch_cumusum(int dop, int in_dt, ScanArgs g, cudaStream_t s);
+size_t scan_acc_size(int dop, int in_dt, int f32_comp);
+
+}  // namespace pg
+
+namespace pg {
+// ----------------------------------------------------------------- inner
+struct InnerArgs {
+  const char *a, *b;
+  char *c;
+  int64_t n, inc_a, inc_b, rows;
+  Loop L;  // pdl 0 a, 1 b, 2 c
+  int bad;
+  uint64_t abad, bbad, cbad;
+  int abad_isnan, bbad_isnan;
+  int *setbad;
+  int group;
+};
+pdlgb300_error launch_inner(int dt, const InnerArgs &g, cudaStream_t s);
+
+// --------------------------------------------------------------- matmult
+struct MMArgs {
+  const char *a, *b;
+  char *c;
+  int64_t K, M, N;                 // t, h, w
+  int64_t a_k, a_m, b_n, b_k, c_n, c_m;  // element increments
+  int64_t batch;
+  Loop L;  // batch dims: pdl 0 a, 1 b, 2 c
+  int bad;
+  uint64_t abad, bbad, cbad;
+  int abad_isnan, bbad_isnan, cbad_isnan;
+};
+// mode: PDLGB300_MATMULT_* (float32 only; other types use the exact kernel)
+pdlgb300_error launch_matmult_simt(int dt, int fused, const MMArgs &g, cudaStream_t s);
+pdlgb300_error launch_matmult_tc(int limbs, const MMArgs &g, cudaStream_t s);
+bool matmult_tc_supported(const MMArgs &g);
+
+// ------------------------------------------- fused sumover(mult+plus)
+struct FusedArgs {
+  const char *a, *b, *d;
+  char *c;
+  int64_t n, inc_a, inc_b, inc_d, rows;
+  Loop L;  // pdl 0 a, 1 b, 2 d, 3 c
+  int fa, fb, fd;                  // input badflag states
+  uint64_t abad, bbad, dbad, tbad, ubad, cbad;
+  int abad_isnan, bbad_isnan, dbad_isnan, tbad_isnan, ubad_isnan;
+  int f32_comp;
+  int outer;                       // 1: a/d vary with dim ky only, b with dim jx only
+  int d_is_a;                      // d aliases a (same data and increments)
+  int jdim, kdim;                  // loop dims of the outer pattern
+};
+pdlgb300_error launch_fused_smp(int dt, const FusedArgs &g, cudaStream_t s);
+
+// ------------------------------------------------------------ adjoints
+struct UnbArgs {  // out(o) = sum over r of f(in(o, r))
+  const char *x, *y;               // y optional (mult_bwd multiplies by y)
+  char *out;
+  Loop Lo;                         // output index space: pdl 0 x, 1 y, 2 out
+  Loop Lr;                         // reduced index space: pdl 0 x, 1 y
+  double scale;
+};
+pdlgb300_error launch_unbroadcast(int dt, const UnbArgs &g, cudaStream_t s);
+}  // namespace pg

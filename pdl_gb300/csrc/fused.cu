@@ -1,0 +1,235 @@
+// fused.cu -- sumover(plus(mult(a, b), d)) in one pass: c() over a(n), b(n),
+// d(n), each element computed exactly as the three reference ops compute it
+// in sequence (lib/PDL/Ops.pd:133-153 for mult and plus with their bad-value
+// rules, lib/PDL/Ufunc.pd:94-118 for sumover), without materialising the
+// broadcast intermediates a*b and a*b+d.
+//
+// The common shape (a and d vary along one output dim, b along the other:
+// an outer-product broadcast such as a(n,1,K) * b(n,J,1)) is tiled like a
+// GEMM: each block owns 64x64 outputs, stages 32-deep slabs of a, b (and d)
+// in shared memory, and each thread accumulates a 4x4 output tile, so every
+// input element read from HBM is reused 64 times.  Integer work is order
+// free and exact; float32 sums use compensated accumulation.
+#include "args.cuh"
+#include "f64sum.cuh"
+
+namespace pg {
+namespace {
+
+template <class T, class Out, bool COMP> struct FAcc {
+  using A = std::conditional_t<
+      std::is_integral_v<Out>, uns_t<Out>,
+      std::conditional_t<std::is_same_v<Out, float>,
+                         std::conditional_t<COMP, float2, float>, double>>;
+  __device__ static A zero() {
+    A a;
+    memset(&a, 0, sizeof a);
+    return a;
+  }
+  __device__ static void add(A &a, T u) {
+    if constexpr (std::is_integral_v<Out>) {
+      a += (A)(Out)u;
+    } else if constexpr (std::is_same_v<A, float2>) {
+      float x = (float)u;
+      float s = __fadd_rn(a.x, x);
+      float bp = __fsub_rn(s, a.x);
+      float e = __fadd_rn(__fsub_rn(a.x, __fsub_rn(s, bp)), __fsub_rn(x, bp));
+      a.x = s;
+      a.y = __fadd_rn(a.y, e);
+    } else {
+      a = rn_add(a, (A)u);
+    }
+  }
+  __device__ static Out value(const A &a) {
+    if constexpr (std::is_same_v<A, float2>) return __fadd_rn(a.x, a.y);
+    else return (Out)a;
+  }
+};
+
+// One element of the chain.  Returns false when the element is skipped.
+template <class T, bool BAD>
+__device__ __forceinline__ bool chain(const FusedArgs &g, T va, T vb, T vd, const Bad<T> &ba,
+                                      const Bad<T> &bb, const Bad<T> &bd, const Bad<T> &bt,
+                                      T tbad, T ubad, T &u) {
+  if constexpr (!BAD) {
+    u = op_add<T>(op_mul<T>(va, vb), vd);
+    return true;
+  } else {
+    const bool ft = g.fa || g.fb, fu = ft || g.fd;
+    T t = ((g.fa && ba.is(va)) || (g.fb && bb.is(vb))) ? tbad : op_mul<T>(va, vb);
+    u = ((ft && bt.is(t)) || (g.fd && bd.is(vd))) ? ubad : op_add<T>(t, vd);
+    return !(fu && bt.is(u));  // sumover skips bad u (u's badvalue: the default)
+  }
+}
+
+constexpr int FJ = 64, FK = 64, FT = 256;
+
+template <class T, class Out, bool BAD, bool COMP, bool DA>
+__global__ void __launch_bounds__(FT) k_fused_outer(const FusedArgs g) {
+  using FA = FAcc<T, Out, COMP>;
+  // slab depth; rows padded by one element so the transposing stores
+  // (consecutive n across lanes) hit distinct banks
+  constexpr int FN = sizeof(T) == 8 ? 16 : 32;
+  __shared__ T sa[FN][FK + 1];
+  __shared__ T sb[FN][FJ + 1];
+  __shared__ T sd[DA ? 1 : FN][DA ? 1 : FK + 1];
+  const int tid = threadIdx.x, tj = tid % 16, tk = tid / 16;
+  const int64_t J = g.L.size[g.jdim], K = g.L.size[g.kdim];
+  const int64_t j0 = (int64_t)blockIdx.x * FJ, k0 = (int64_t)blockIdx.y * FK;
+  const int64_t a_k = g.L.inc[0][g.kdim], b_j = g.L.inc[1][g.jdim];
+  const int64_t d_k = g.L.inc[2][g.kdim], d_j = g.L.inc[2][g.jdim];
+  const T *A = reinterpret_cast<const T *>(g.a);
+  const T *B = reinterpret_cast<const T *>(g.b);
+  const T *D = reinterpret_cast<const T *>(g.d);
+  Bad<T> ba{from_bits<T>(g.abad), (bool)g.abad_isnan};
+  Bad<T> bb{from_bits<T>(g.bbad), (bool)g.bbad_isnan};
+  Bad<T> bd{from_bits<T>(g.dbad), (bool)g.dbad_isnan};
+  Bad<T> bt{from_bits<T>(g.tbad), (bool)g.tbad_isnan};
+  const T tbad = from_bits<T>(g.tbad), ubad = from_bits<T>(g.ubad);
+  typename FA::A acc[4][4];
+  int cnt[4][4];
+#pragma unroll
+  for (int x = 0; x < 4; x++)
+#pragma unroll
+    for (int y = 0; y < 4; y++) {
+      acc[x][y] = FA::zero();
+      cnt[x][y] = 0;
+    }
+  for (int64_t i0 = 0; i0 < g.n; i0 += FN) {
+    __syncthreads();
+    // stage: FN x FK of a (and d), FN x FJ of b; i fastest across threads
+    for (int idx = tid; idx < FN * FK; idx += FT) {
+      int i = idx % FN, k = idx / FN;
+      int64_t gi = i0 + i, gk = k0 + k;
+      bool in = gi < g.n && gk < K;
+      sa[i][k] = in ? A[gi * g.inc_a + gk * a_k] : (T)0;
+      if constexpr (!DA) sd[i][k] = in ? D[gi * g.inc_d + gk * d_k] : (T)0;
+    }
+    for (int idx = tid; idx < FN * FJ; idx += FT) {
+      int i = idx % FN, j = idx / FN;
+      int64_t gi = i0 + i, gj = j0 + j;
+      sb[i][j] = (gi < g.n && gj < J) ? B[gi * g.inc_b + gj * b_j] : (T)0;
+    }
+    __syncthreads();
+    const int iend = (int)(g.n - i0 < FN ? g.n - i0 : FN);
+    for (int i = 0; i < iend; i++) {
+      T av[4], bv[4], dv[4];
+#pragma unroll
+      for (int x = 0; x < 4; x++) {
+        av[x] = sa[i][tk * 4 + x];
+        bv[x] = sb[i][tj * 4 + x];
+        if constexpr (DA) dv[x] = av[x];
+        else dv[x] = sd[i][tk * 4 + x];
+      }
+      if constexpr (!BAD && DA && std::is_integral_v<T>) {
+        // a*b + a == a*(b+1) in wrapping arithmetic: one multiply-add
+#pragma unroll
+        for (int y = 0; y < 4; y++) {
+          T b1 = wadd<T>(bv[y], (T)1);
+#pragma unroll
+          for (int x = 0; x < 4; x++) FA::add(acc[y][x], wmul<T>(av[x], b1));
+        }
+      } else {
+#pragma unroll
+        for (int y = 0; y < 4; y++)
+#pragma unroll
+          for (int x = 0; x < 4; x++) {
+            T u;
+            if (chain<T, BAD>(g, av[x], bv[y], dv[x], ba, bb, bd, bt, tbad, ubad, u)) {
+              FA::add(acc[y][x], u);
+              if (BAD) cnt[y][x]++;
+            }
+          }
+      }
+    }
+  }
+  // write c(j, k): c's inc along the j dim and the k dim
+  const int64_t c_j = g.L.inc[3][g.jdim], c_k = g.L.inc[3][g.kdim];
+  Out *C = reinterpret_cast<Out *>(g.c);
+  const Out cbad = from_bits<Out>(g.cbad);
+#pragma unroll
+  for (int y = 0; y < 4; y++) {
+    int64_t j = j0 + tj * 4 + y;
+    if (j >= J) continue;
+#pragma unroll
+    for (int x = 0; x < 4; x++) {
+      int64_t k = k0 + tk * 4 + x;
+      if (k >= K) continue;
+      Out r = (BAD && cnt[y][x] == 0) ? cbad : FA::value(acc[y][x]);
+      C[j * c_j + k * c_k] = r;
+    }
+  }
+}
+
+template <class T, class Out, bool BAD, bool COMP>
+__global__ void k_fused_thread(const FusedArgs g) {
+  using FA = FAcc<T, Out, COMP>;
+  Bad<T> ba{from_bits<T>(g.abad), (bool)g.abad_isnan};
+  Bad<T> bb{from_bits<T>(g.bbad), (bool)g.bbad_isnan};
+  Bad<T> bd{from_bits<T>(g.dbad), (bool)g.dbad_isnan};
+  Bad<T> bt{from_bits<T>(g.tbad), (bool)g.tbad_isnan};
+  const T tbad = from_bits<T>(g.tbad), ubad = from_bits<T>(g.ubad);
+  const Out cbad = from_bits<Out>(g.cbad);
+  for (int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; row < g.rows;
+       row += (int64_t)gridDim.x * blockDim.x) {
+    int64_t offs[MAXP];
+    loop_offsets(g.L, row, offs);
+    const T *a = reinterpret_cast<const T *>(g.a) + offs[0];
+    const T *b = reinterpret_cast<const T *>(g.b) + offs[1];
+    const T *d = reinterpret_cast<const T *>(g.d) + offs[2];
+    auto acc = FA::zero();
+    int64_t cnt = 0;
+    for (int64_t i = 0; i < g.n; i++) {
+      T u;
+      if (chain<T, BAD>(g, a[i * g.inc_a], b[i * g.inc_b], d[i * g.inc_d], ba, bb, bd, bt,
+                        tbad, ubad, u)) {
+        FA::add(acc, u);
+        cnt++;
+      }
+    }
+    Out *c = reinterpret_cast<Out *>(g.c) + offs[3];
+    *c = (BAD && cnt == 0) ? cbad : FA::value(acc);
+  }
+}
+
+template <class T, class Out, bool COMP>
+pdlgb300_error fused_typed(const FusedArgs &g, cudaStream_t s) {
+  pdlgb300_error e = pgh::ok();
+  if (g.rows == 0) return e;
+  const bool bad = g.fa || g.fb || g.fd;
+  if (g.outer) {
+    dim3 grid((unsigned)((g.L.size[g.jdim] + FJ - 1) / FJ),
+              (unsigned)((g.L.size[g.kdim] + FK - 1) / FK));
+    if (bad) {
+      if (g.d_is_a) k_fused_outer<T, Out, true, COMP, true><<<grid, FT, 0, s>>>(g);
+      else k_fused_outer<T, Out, true, COMP, false><<<grid, FT, 0, s>>>(g);
+    } else {
+      if (g.d_is_a) k_fused_outer<T, Out, false, COMP, true><<<grid, FT, 0, s>>>(g);
+      else k_fused_outer<T, Out, false, COMP, false><<<grid, FT, 0, s>>>(g);
+    }
+    if (!pgh::cuda_check(cudaGetLastError(), &e, "k_fused_outer")) return e;
+    pgh::record_kernel("k_fused_outer", (int64_t)grid.x * grid.y, FT);
+    return e;
+  }
+  int64_t grid = std::min<int64_t>((g.rows + 127) / 128, (int64_t)pgh::num_sms() * 64);
+  if (bad) k_fused_thread<T, Out, true, COMP><<<(int)grid, 128, 0, s>>>(g);
+  else k_fused_thread<T, Out, false, COMP><<<(int)grid, 128, 0, s>>>(g);
+  if (!pgh::cuda_check(cudaGetLastError(), &e, "k_fused_thread")) return e;
+  pgh::record_kernel("k_fused_thread", grid, 128);
+  return e;
+}
+
+}  // namespace
+
+pdlgb300_error launch_fused_smp(int dt, const FusedArgs &g, cudaStream_t s) {
+  PG_DISPATCH(dt, {
+    using T = typename TT<DT>::T;
+    using Out = typename TT<intplus(DT)>::T;
+    if constexpr (std::is_same_v<Out, float>)
+      if (g.f32_comp) return fused_typed<T, Out, true>(g, s);
+    return fused_typed<T, Out, false>(g, s);
+  });
+  return pgh::err(PDLGB300_EUSERERROR, "sumover_mult_plus: unsupported type %d", dt);
+}
+
+}  // namespace pg

@@ -1,0 +1,481 @@
+// reduce.cuh -- the PDL::Ufunc reductions over dim 0 (a(n) -> b()) as
+// GB300 kernels.  Semantics per op follow lib/PDL/Ufunc.pd:
+//   sumover/dsumover :94-118, prodover/dprodover :91-118 (leftzero),
+//   average/daverage :413-444, minimum/maximum :446-475,
+//   minimum_ind/maximum_ind :477-500.
+// Rows (one output each) are the collapsed broadcast dims; the reduced dim
+// n is walked by a group of threads (contiguous n: 16-byte vector loads) or
+// by one thread (strided n, the reference's own sequential order).
+#pragma once
+#include "args.cuh"
+#include "f64sum.cuh"
+
+namespace pg {
+
+
+// ---------------------------------------------------------------- accums
+
+// Float-float (compensated) float32 accumulator: TwoSum per element.
+struct FF {
+  float hi, lo;
+};
+__device__ __forceinline__ void ff_add(FF &a, float x) {
+  float s = __fadd_rn(a.hi, x);
+  float bp = __fsub_rn(s, a.hi);
+  float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bp)), __fsub_rn(x, bp));
+  a.hi = s;
+  a.lo = __fadd_rn(a.lo, e);
+}
+__device__ __forceinline__ void ff_merge(FF &a, const FF &b) {
+  float s = __fadd_rn(a.hi, b.hi);
+  float bp = __fsub_rn(s, a.hi);
+  float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bp)), __fsub_rn(b.hi, bp));
+  e = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
+  float h = __fadd_rn(s, e);
+  a.lo = __fsub_rn(e, __fsub_rn(h, s));
+  a.hi = h;
+}
+
+// Sum of In into Out.  Integers wrap in Out's width (order-free, so exact);
+// float32 is compensated or plain; float64 uses F64Sum (exact-within-block
+// integer alignment plus FP64 adds, no less accurate than FP64).
+template <class In, class Out, bool COMP> struct SumAcc {
+  using Acc = std::conditional_t<
+      std::is_integral_v<Out>, uns_t<Out>,
+      std::conditional_t<std::is_same_v<Out, float>,
+                         std::conditional_t<COMP, FF, float>,
+                         std::conditional_t<std::is_same_v<In, double>, F64Sum, double>>>;
+  __device__ static Acc init() {
+    Acc a;
+    memset(&a, 0, sizeof a);
+    return a;
+  }
+  __device__ static void add(Acc &a, In v) {
+    if constexpr (std::is_integral_v<Out>) {
+      a += (Acc)(Out)v;
+    } else if constexpr (std::is_same_v<Acc, FF>) {
+      ff_add(a, (float)v);
+    } else if constexpr (std::is_same_v<Acc, F64Sum>) {
+      a.add_fp64(v);
+    } else {
+      a = rn_add(a, (Acc)v);
+    }
+  }
+  __device__ static void merge(Acc &a, const Acc &b) {
+    if constexpr (std::is_integral_v<Out>) a += b;
+    else if constexpr (std::is_same_v<Acc, FF>) ff_merge(a, b);
+    else if constexpr (std::is_same_v<Acc, F64Sum>) a.merge(b);
+    else a = rn_add(a, b);
+  }
+  __device__ static Out value(const Acc &a) {
+    if constexpr (std::is_integral_v<Out>) return (Out)a;
+    else if constexpr (std::is_same_v<Acc, FF>) return __fadd_rn(a.hi, a.lo);
+    else if constexpr (std::is_same_v<Acc, F64Sum>) return a.value();
+    else return (Out)a;
+  }
+};
+
+// --------------------------------------------------------------------- ops
+// Each op: Acc, init, add(acc, v, idx), merge(a, b) (a holds lower indices),
+// finalize(acc, cnt, bad, badval, &setbad) -> Out, kCount (needs good count).
+
+template <class In, class Out, bool COMP> struct OpSum {
+  using S = SumAcc<In, Out, COMP>;
+  using Acc = typename S::Acc;
+  static constexpr bool kCount = false, kVec = true;
+  static constexpr bool kBlock = std::is_same_v<Acc, F64Sum>;
+  static constexpr int kU = kBlock ? 8 : 0;
+  template <int B> __device__ static void add_block(Acc &a, const In *v) {
+    if constexpr (kBlock) a.template add_block<B>(v);
+  }
+  __device__ static Acc init() { return S::init(); }
+  __device__ static void add(Acc &a, In v, int64_t) { S::add(a, v); }
+  template <int VEC> __device__ static void add_vec(Acc &a, const In *v, int64_t) {
+    if constexpr (std::is_same_v<Acc, F64Sum> && VEC == 2) a.add_block2(v);
+    else {
+#pragma unroll
+      for (int e = 0; e < VEC; e++) S::add(a, v[e]);
+    }
+  }
+  __device__ static void merge(Acc &a, const Acc &b) { S::merge(a, b); }
+  __device__ static Out fin(const Acc &a, int64_t cnt, bool bad, Out badval, int *) {
+    if (bad && cnt == 0) return badval;
+    return S::value(a);
+  }
+};
+
+template <class In, class Out> struct OpProd {
+  using Acc = std::conditional_t<std::is_integral_v<Out>, uns_t<Out>, Out>;
+  static constexpr bool kCount = false, kVec = true, kBlock = false;
+  static constexpr int kU = 0;
+  template <int B> __device__ static void add_block(Acc &, const In *) {}
+  __device__ static Acc init() { return (Acc)1; }
+  __device__ static void add(Acc &a, In v, int64_t) {
+    if constexpr (std::is_integral_v<Out>) a = (Acc)wmul<Out>((Out)a, (Out)v);
+    else a = rn_mul(a, (Out)v);
+  }
+  template <int VEC> __device__ static void add_vec(Acc &a, const In *v, int64_t i) {
+#pragma unroll
+    for (int e = 0; e < VEC; e++) add(a, v[e], i + e);
+  }
+  __device__ static void merge(Acc &a, const Acc &b) {
+    if constexpr (std::is_integral_v<Out>) a = (Acc)wmul<Out>((Out)a, (Out)b);
+    else a = rn_mul(a, b);
+  }
+  __device__ static Out fin(const Acc &a, int64_t cnt, bool bad, Out badval, int *) {
+    if (bad && cnt == 0) return badval;
+    return (Out)a;
+  }
+};
+
+template <class In, class Out, bool COMP> struct OpAvg {
+  using S = SumAcc<In, Out, COMP>;
+  using Acc = typename S::Acc;
+  static constexpr bool kCount = true, kVec = true;
+  static constexpr bool kBlock = std::is_same_v<Acc, F64Sum>;
+  static constexpr int kU = kBlock ? 8 : 0;
+  template <int B> __device__ static void add_block(Acc &a, const In *v) {
+    if constexpr (kBlock) a.template add_block<B>(v);
+  }
+  __device__ static Acc init() { return S::init(); }
+  __device__ static void add(Acc &a, In v, int64_t) { S::add(a, v); }
+  template <int VEC> __device__ static void add_vec(Acc &a, const In *v, int64_t) {
+    if constexpr (std::is_same_v<Acc, F64Sum> && VEC == 2) a.add_block2(v);
+    else {
+#pragma unroll
+      for (int e = 0; e < VEC; e++) S::add(a, v[e]);
+    }
+  }
+  __device__ static void merge(Acc &a, const Acc &b) { S::merge(a, b); }
+  __device__ static Out fin(const Acc &a, int64_t cnt, bool bad, Out badval, int *) {
+    if (cnt == 0) {
+      if (bad) return badval;
+      if constexpr (std::is_floating_point_v<Out>) return (Out)NAN; else return (Out)0;
+    }
+    Out tmp = S::value(a);
+    // `tmp / cnt` with cnt a PDL_Indx: C's usual arithmetic conversions.
+    if constexpr (std::is_floating_point_v<Out>) {
+      return tmp / (Out)cnt;
+    } else if constexpr (std::is_same_v<Out, uint64_t>) {
+      return tmp / (uint64_t)cnt;
+    } else {
+      return (Out)((int64_t)tmp / cnt);
+    }
+  }
+};
+
+// minimum/maximum(+_ind): the sequential rule "replace when first, when
+// a OP cur, or when cur is NaN" equals the total order: non-NaN beats NaN;
+// among non-NaN the smaller (larger) value, ties to the lower index; among
+// NaNs the higher index.  That order is associative, so any split works.
+template <class T> struct MMAcc {
+  int64_t idx;  // -1: empty
+  T v;
+};
+template <class T, bool MAX, bool IND> struct OpMM {
+  using Acc = MMAcc<T>;
+  using Out = std::conditional_t<IND, int64_t, T>;
+  static constexpr bool kCount = false, kVec = true, kBlock = false;
+  static constexpr int kU = 0;
+  template <int B> __device__ static void add_block(Acc &, const T *) {}
+  __device__ static Acc init() { return Acc{-1, (T)0}; }
+  __device__ static bool better(T x, int64_t ix, T y, int64_t iy) {
+    // does (x, ix) replace (y, iy)?  (ix > iy in sequential order)
+    bool xn = isnan_any(x), yn = isnan_any(y);
+    if (yn) return !xn || ix > iy;
+    if (xn) return false;
+    if constexpr (MAX) return x > y || (x == y && ix < iy);
+    else return x < y || (x == y && ix < iy);
+  }
+  __device__ static void add(Acc &a, T v, int64_t i) {
+    if (a.idx < 0 || better(v, i, a.v, a.idx)) { a.v = v; a.idx = i; }
+  }
+  template <int VEC> __device__ static void add_vec(Acc &a, const T *v, int64_t i) {
+#pragma unroll
+    for (int e = 0; e < VEC; e++) add(a, v[e], i + e);
+  }
+  __device__ static void merge(Acc &a, const Acc &b) {
+    if (b.idx < 0) return;
+    if (a.idx < 0 || better(b.v, b.idx, a.v, a.idx)) a = b;
+  }
+  __device__ static Out fin(const Acc &a, int64_t, bool, Out badval, int *setbad) {
+    if (a.idx < 0) {
+      *setbad = 1;  // $SETBAD(c()); $PDLSTATESETBAD(c) even without bad mode
+      return badval;
+    }
+    if constexpr (IND) return a.idx; else return a.v;
+  }
+};
+
+// ------------------------------------------------------------- reductions
+
+template <class Acc> struct AccCnt {
+  Acc acc;
+  int64_t cnt;
+};
+
+template <class Op>
+__device__ __forceinline__ void merge_ac(AccCnt<typename Op::Acc> &x,
+                                         const AccCnt<typename Op::Acc> &y) {
+  Op::merge(x.acc, y.acc);
+  x.cnt += y.cnt;
+}
+
+// Reduce across the G threads of a group; G is 32 (a warp; several rows per
+// block) or blockDim.x (one row per block).  Result valid in lane 0.
+template <class Op>
+__device__ __forceinline__ AccCnt<typename Op::Acc> group_reduce(
+    AccCnt<typename Op::Acc> v, int G) {
+  using AC = AccCnt<typename Op::Acc>;
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) {
+    AC o;
+    o.acc = shfl_down_any(v.acc, d);
+    o.cnt = __shfl_down_sync(0xffffffffu, v.cnt, d);
+    merge_ac<Op>(v, o);
+  }
+  if (G <= 32) return v;
+  __shared__ AC sm[32];
+  int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) sm[w] = v;
+  __syncthreads();
+  if (w == 0) {
+    int nw = blockDim.x >> 5;
+    v = l < nw ? sm[l] : AC{Op::init(), 0};
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+      AC o;
+      o.acc = shfl_down_any(v.acc, d);
+      o.cnt = __shfl_down_sync(0xffffffffu, v.cnt, d);
+      merge_ac<Op>(v, o);
+    }
+  }
+  return v;
+}
+
+template <class In, int VEC> struct alignas(16) VecT {
+  In e[VEC];
+};
+
+// 16-byte streaming load (read once: evict-first).
+template <class V> __device__ __forceinline__ V ldv(const V *p) {
+  static_assert(sizeof(V) == 16, "16-byte vectors");
+  float4 f = __ldcs(reinterpret_cast<const float4 *>(p));
+  V v;
+  memcpy(&v, &f, 16);
+  return v;
+}
+
+// Accumulate elements [lo, hi) of a contiguous row, G threads, lane `lane`.
+template <class Op, class In, bool BAD>
+__device__ __forceinline__ void row_accumulate(const In *row, int64_t lo, int64_t hi,
+                                               int lane, int G, const Bad<In> &bv,
+                                               AccCnt<typename Op::Acc> &ac) {
+  constexpr int VEC = 16 / sizeof(In);
+  constexpr int U = Op::kU ? Op::kU : (sizeof(In) >= 8 ? 4 : 2);  // vectors in flight
+  int64_t i = lo;
+  // scalar head up to a 16-byte boundary
+  int64_t mis = ((uintptr_t)(row + lo) & 15) / sizeof(In);
+  int64_t head = mis ? (VEC - mis) : 0;
+  if (head > hi - lo) head = hi - lo;
+  if (lane < head) {
+    In v = row[lo + lane];
+    if (!(BAD && bv.is(v))) {
+      Op::add(ac.acc, v, lo + lane);
+      ac.cnt++;
+    }
+  }
+  i = lo + head;
+  const VecT<In, VEC> *vp = reinterpret_cast<const VecT<In, VEC> *>(row + i);
+  int64_t nv = (hi - i) / VEC;
+  for (int64_t k = lane; k < nv; k += (int64_t)G * U) {
+    VecT<In, VEC> buf[U];
+    const bool full = k + (int64_t)(U - 1) * G < nv;
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      int64_t kk = k + (int64_t)u * G;
+      if (full || kk < nv) buf[u] = ldv(vp + kk);
+    }
+    if constexpr (!BAD && Op::kBlock) {
+      if (full) {
+        Op::template add_block<VEC * U>(ac.acc, reinterpret_cast<const In *>(buf));
+        if constexpr (Op::kCount) ac.cnt += VEC * U;
+        continue;
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      int64_t kk = k + (int64_t)u * G;
+      if (full || kk < nv) {
+        int64_t base = i + kk * VEC;
+        if constexpr (BAD) {
+#pragma unroll
+          for (int e = 0; e < VEC; e++) {
+            In v = buf[u].e[e];
+            if (!bv.is(v)) {
+              Op::add(ac.acc, v, base + e);
+              ac.cnt++;
+            }
+          }
+        } else {
+          Op::template add_vec<VEC>(ac.acc, buf[u].e, base);
+          if constexpr (Op::kCount) ac.cnt += VEC;
+        }
+      }
+    }
+  }
+  // scalar tail
+  for (int64_t t = i + nv * VEC + lane; t < hi; t += G) {
+    In v = row[t];
+    if (!(BAD && bv.is(v))) {
+      Op::add(ac.acc, v, t);
+      ac.cnt++;
+    }
+  }
+}
+
+// Accumulate elements [lo, hi) of a strided row (scalar loads).
+template <class Op, class In, bool BAD>
+__device__ __forceinline__ void row_accumulate_strided(const In *row, int64_t inc,
+                                                       int64_t lo, int64_t hi, int lane,
+                                                       int G, const Bad<In> &bv,
+                                                       AccCnt<typename Op::Acc> &ac) {
+  for (int64_t t = lo + lane; t < hi; t += G) {
+    In v = row[t * inc];
+    if (!(BAD && bv.is(v))) {
+      Op::add(ac.acc, v, t);
+      ac.cnt++;
+    }
+  }
+}
+
+template <class Out> __device__ __forceinline__ void store_out(char *p, Out v) {
+  *reinterpret_cast<Out *>(p) = v;
+}
+
+// Group-per-row kernel.  Contiguous n.  nsplit > 1: each block does one
+// chunk of one row and writes its partial accumulator.
+template <class Op, class In, class Out, bool BAD>
+__global__ void __launch_bounds__(512) k_red_rows(const RedArgs args) {
+  using Acc = typename Op::Acc;
+  using AC = AccCnt<Acc>;
+  const int G = args.group;
+  const int lane = G <= 32 ? (threadIdx.x & 31) : threadIdx.x;
+  const int gpb = G <= 32 ? (blockDim.x >> 5) : 1;  // groups per block
+  const int gid = G <= 32 ? (threadIdx.x >> 5) : 0;
+  Bad<In> bv{from_bits<In>(args.abad_bits), (bool)args.abad_isnan};
+  Out obad = from_bits<Out>(args.bbad_bits);
+  const int64_t nunits = args.rows * args.nsplit;
+  for (int64_t u = (int64_t)blockIdx.x * gpb + gid; u < nunits;
+       u += (int64_t)gridDim.x * gpb) {
+    int64_t row = u / args.nsplit;
+    int split = (int)(u - row * args.nsplit);
+    int64_t offs[MAXP];
+    loop_offsets(args.L, row, offs);
+    const In *a = reinterpret_cast<const In *>(args.a) + offs[0];
+    int64_t lo = 0, hi = args.n;
+    if (args.nsplit > 1) {
+      int64_t chunk = (args.n + args.nsplit - 1) / args.nsplit;
+      chunk = (chunk + 31) & ~(int64_t)31;
+      lo = split * chunk;
+      hi = lo + chunk < args.n ? lo + chunk : args.n;
+      if (lo > hi) lo = hi;
+    }
+    AC ac{Op::init(), 0};
+    if (args.inc_n == 1)
+      row_accumulate<Op, In, BAD>(a, lo, hi, lane, G, bv, ac);
+    else
+      row_accumulate_strided<Op, In, BAD>(a, args.inc_n, lo, hi, lane, G, bv, ac);
+    ac = group_reduce<Op>(ac, G);
+    if (lane == 0) {
+      if (args.nsplit > 1) {
+        reinterpret_cast<Acc *>(args.partials)[u] = ac.acc;
+        args.pcounts[u] = ac.cnt;
+      } else {
+        int64_t cnt = (BAD || Op::kCount || args.inc_n != 1) ? ac.cnt : args.n;
+        Out r = Op::fin(ac.acc, cnt, BAD, obad, args.setbad);
+        store_out<Out>(args.b + offs[1] * (int64_t)sizeof(Out), r);
+      }
+    }
+  }
+}
+
+// Combine the per-split partials of each row, in split order.
+template <class Op, class In, class Out, bool BAD>
+__global__ void k_red_combine(const RedArgs args) {
+  using Acc = typename Op::Acc;
+  Out obad = from_bits<Out>(args.bbad_bits);
+  for (int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; row < args.rows;
+       row += (int64_t)gridDim.x * blockDim.x) {
+    const Acc *p = reinterpret_cast<const Acc *>(args.partials) + row * args.nsplit;
+    Acc acc = p[0];
+    int64_t cnt = args.pcounts[row * args.nsplit];
+    for (int s = 1; s < args.nsplit; s++) {
+      Op::merge(acc, p[s]);
+      cnt += args.pcounts[row * args.nsplit + s];
+    }
+    int64_t offs[MAXP];
+    loop_offsets(args.L, row, offs);
+    if (!(BAD || Op::kCount || args.inc_n != 1)) cnt = args.n;
+    Out r = Op::fin(acc, cnt, BAD, obad, args.setbad);
+    store_out<Out>(args.b + offs[1] * (int64_t)sizeof(Out), r);
+  }
+}
+
+// Thread-per-row kernel: any increments, the reference's sequential order
+// along n.  Adjacent threads take adjacent rows (coalesced when the
+// innermost broadcast dim is contiguous).
+template <class Op, class In, class Out, bool BAD>
+__global__ void k_red_thread(const RedArgs args) {
+  Bad<In> bv{from_bits<In>(args.abad_bits), (bool)args.abad_isnan};
+  Out obad = from_bits<Out>(args.bbad_bits);
+  for (int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; row < args.rows;
+       row += (int64_t)gridDim.x * blockDim.x) {
+    int64_t offs[MAXP];
+    loop_offsets(args.L, row, offs);
+    const In *a = reinterpret_cast<const In *>(args.a) + offs[0];
+    AccCnt<typename Op::Acc> ac{Op::init(), 0};
+    for (int64_t i = 0; i < args.n; i++) {
+      In v = a[i * args.inc_n];
+      if (BAD && bv.is(v)) continue;
+      Op::add(ac.acc, v, i);
+      ac.cnt++;
+    }
+    Out r = Op::fin(ac.acc, ac.cnt, BAD, obad, args.setbad);
+    store_out<Out>(args.b + offs[1] * (int64_t)sizeof(Out), r);
+  }
+}
+
+template <class Op, class In, class Out>
+pdlgb300_error launch_red_typed(RedArgs args, const RedLaunch &lc, cudaStream_t s) {
+  pdlgb300_error e = pgh::ok();
+  const char *nm = "k_red";
+  if (lc.kind == 1) {
+    if (args.bad) k_red_thread<Op, In, Out, true><<<lc.grid, lc.block, 0, s>>>(args);
+    else k_red_thread<Op, In, Out, false><<<lc.grid, lc.block, 0, s>>>(args);
+    nm = "k_red_thread";
+  } else {
+    if (args.bad) k_red_rows<Op, In, Out, true><<<lc.grid, lc.block, 0, s>>>(args);
+    else k_red_rows<Op, In, Out, false><<<lc.grid, lc.block, 0, s>>>(args);
+    nm = "k_red_rows";
+    if (args.nsplit > 1) {
+      if (!pgh::cuda_check(cudaGetLastError(), &e, nm)) return e;
+      pgh::record_kernel(nm, lc.grid, lc.block);
+      int g = (int)std::min<int64_t>((args.rows + 127) / 128, 65535);
+      if (args.bad) k_red_combine<Op, In, Out, true><<<g, 128, 0, s>>>(args);
+      else k_red_combine<Op, In, Out, false><<<g, 128, 0, s>>>(args);
+      nm = "k_red_combine";
+      if (!pgh::cuda_check(cudaGetLastError(), &e, nm)) return e;
+      pgh::record_kernel(nm, g, 128);
+      return e;
+    }
+  }
+  if (!pgh::cuda_check(cudaGetLastError(), &e, nm)) return e;
+  pgh::record_kernel(nm, lc.grid, lc.block);
+  return e;
+}
+
+template <class Op> size_t acc_size() { return sizeof(typename Op::Acc); }
+
+}  // namespace pg

@@ -1,0 +1,344 @@
+"""GPU parity: every op of the path through the C ABI against the oracle on
+the same seeded inputs.
+
+Bar: integer results, indices, bad masks and badflags bit-exact; float
+results bit-exact where the GPU keeps the reference's order and rounding
+(plus, mult, min/max, exact-mode matmult), otherwise within the stated
+bound of the reference's own rounding error:
+  sums / averages / running sums:  |g-e| <= (n+2) * eps * sum|a|
+  products:                         |g-e| <= (n+2) * eps * |e|  (+ tiny)
+  inner:                            |g-e| <= (n+2) * eps * sum|a*b|
+where eps is the unit roundoff of the accumulating type (float32 results
+are compared against the reference's plain float32 loop, which carries
+that error; the GPU's compensated sum carries less)."""
+import numpy as np
+import pytest
+
+import pdl_gb300 as P
+from helpers import (FLOAT_TYPES, INT_TYPES, REAL_TYPES, assert_same, rand_array,
+                     seeded, to_pdl)
+from oracle import oracle as O
+from pdl_gb300.ndarray import NP_DTYPES, type_code
+
+pytestmark = pytest.mark.gpu
+
+EPS = {"float": 2.0 ** -24, "double": 2.0 ** -53}
+RED_OPS = ["sumover", "dsumover", "prodover", "dprodover", "average", "daverage",
+           "minimum", "maximum", "minimum_ind", "maximum_ind", "cumusumover", "dcumusumover"]
+SHAPES = [(7,), (1,), (0,), (0, 3), (5, 0), (3, 4), (17, 33, 2), (257, 5), (1500, 3),
+          (4096, 12), (20000, 2)]
+
+
+def _tol(op, x_np, exp, out_type):
+    """(rtol, atol, scale) for float outputs."""
+    n = x_np.shape[-1] if x_np.ndim else 1
+    acc = "double" if op.startswith("d") or out_type == "double" else "float"
+    eps = EPS[acc]
+    a = np.abs(np.nan_to_num(x_np.astype(np.float64), nan=0.0, posinf=0, neginf=0))
+    if op in ("sumover", "dsumover", "average", "daverage"):
+        scale = a.sum(axis=-1) if a.ndim else a
+        if op.endswith("average"):
+            scale = scale / max(n, 1)
+        return (n + 2) * eps, 1e-300, scale
+    if op in ("cumusumover", "dcumusumover"):
+        return (n + 2) * eps, 1e-300, np.cumsum(a, axis=-1)
+    if op in ("prodover", "dprodover"):
+        return (n + 2) * eps, 1e-290 if acc == "double" else 1e-36, None
+    return 0.0, 0.0, None
+
+
+def _run_both(op, xs, **kw):
+    fn = getattr(P, op)
+    got = fn(*xs, **kw)
+    exp = O.run(op, xs)[0]
+    return got, exp
+
+
+@pytest.mark.parametrize("t", REAL_TYPES)
+@pytest.mark.parametrize("op", RED_OPS)
+def test_reductions_all_types(gpu, op, t):
+    rng = seeded(hash((op, t)) % 2**32)
+    for shape in SHAPES:
+        if op in ("prodover", "dprodover") and t in FLOAT_TYPES:
+            lo, hi = -1.6, 1.6
+        elif op in ("prodover", "dprodover"):
+            lo, hi = -3, 3
+        else:
+            lo, hi = -100, 100
+        a, _ = rand_array(rng, t, shape[::-1], lo, hi)
+        x = to_pdl(a, t)
+        got, exp = _run_both(op, [x])
+        rtol, atol, scale = _tol(op, a, exp, exp.type) if exp.type in FLOAT_TYPES else (0, 0, None)
+        assert_same(got, exp, rtol=rtol, atol=atol, scale=scale, what=f"{op} {t} {shape}")
+
+
+@pytest.mark.parametrize("t", REAL_TYPES)
+@pytest.mark.parametrize("op", RED_OPS)
+def test_reductions_bad_values(gpu, op, t):
+    rng = seeded(hash((op, t, "bad")) % 2**32)
+    for shape in [(9, 4), (300, 7), (5000, 3), (3, 1)]:
+        lo, hi = (-1.6, 1.6) if "prod" in op and t in FLOAT_TYPES else ((-3, 3) if "prod" in op else (-100, 100))
+        a, bad = rand_array(rng, t, shape[::-1], lo, hi, bad_frac=0.2)
+        a[0, :] = P.default_badvalue(type_code(t))  # an all-bad row
+        x = to_pdl(a, t, badflag=True)
+        got, exp = _run_both(op, [x])
+        clean = np.where(bad | (a == P.default_badvalue(type_code(t))), 0, a)
+        rtol, atol, scale = _tol(op, clean, exp, exp.type) if exp.type in FLOAT_TYPES else (0, 0, None)
+        assert_same(got, exp, rtol=rtol, atol=atol, scale=scale, what=f"{op} {t} bad {shape}")
+
+
+@pytest.mark.parametrize("op", ["minimum", "maximum", "minimum_ind", "maximum_ind"])
+@pytest.mark.parametrize("t", FLOAT_TYPES)
+def test_minmax_nan_rules(gpu, op, t):
+    rng = seeded(7)
+    a, _ = rand_array(rng, t, (64, 333), -5, 5, special=True)
+    a[3, :] = np.nan                        # all NaN: the last NaN's index
+    a[4, ::2] = np.nan
+    a[5, :] = 1.0                           # ties: the first index
+    a[6, 10] = -0.0
+    a[6, 11] = 0.0
+    got, exp = _run_both(op, [to_pdl(a, t)])
+    assert_same(got, exp, what=f"{op} {t}")
+
+
+@pytest.mark.parametrize("t", ["double", "float", "long", "byte"])
+@pytest.mark.parametrize("op", ["sumover", "minimum_ind", "cumusumover", "average", "prodover"])
+def test_reductions_on_views(gpu, op, t):
+    """vaffine inputs: transposed (strided n), reversed (negative incs),
+    dummy (zero incs) and sliced views reach the kernels as increments."""
+    rng = seeded(11)
+    a, _ = rand_array(rng, t, (40, 30, 6), -3 if "prod" in op else -50, 3 if "prod" in op else 50)
+    base = to_pdl(a, t)
+    views = [base.xchg(0, 1), base.slice(slice(None, None, -1)), base.slice(slice(1, 29, 3), 4),
+             base.dummy(1, 3), base.xchg(0, 2), base.slice(slice(None), slice(None, None, -2))]
+    for v in views:
+        got, exp = _run_both(op, [v])
+        rtol, atol, scale = (0, 0, None)
+        if exp.type in FLOAT_TYPES:
+            rtol, atol, scale = _tol(op, v.numpy(), exp, exp.type)
+        assert_same(got, exp, rtol=rtol, atol=atol, scale=scale, what=f"{op} {t} view {v.dims}")
+
+
+@pytest.mark.parametrize("op", ["sumover", "average", "minimum", "maximum_ind", "prodover",
+                                "cumusumover", "dsumover"])
+@pytest.mark.parametrize("t", ["double", "float", "long"])
+def test_long_rows_split(gpu, op, t):
+    """Few very long rows take the multi-block split (partials in scratch)."""
+    rng = seeded(3)
+    n = 300_000
+    lo, hi = (-1.2, 1.2) if "prod" in op else (-10, 10)
+    a, _ = rand_array(rng, t, (3, n), lo, hi)
+    x = to_pdl(a, t)
+    got, exp = _run_both(op, [x])
+    rtol, atol, scale = _tol(op, a, exp, exp.type) if exp.type in FLOAT_TYPES else (0, 0, None)
+    assert_same(got, exp, rtol=rtol, atol=atol, scale=scale, what=f"{op} {t} split")
+
+
+def test_device_resident_matches_host_staged(gpu):
+    rng = seeded(5)
+    a, _ = rand_array(rng, "double", (512, 1000), -1, 1)
+    h = to_pdl(a, "double")
+    d = to_pdl(a, "double").to_device()
+    for op in ["sumover", "minimum_ind", "cumusumover"]:
+        r1, r2 = getattr(P, op)(h), getattr(P, op)(d)
+        assert r2.on_device
+        assert np.array_equal(r1.numpy(), r2.numpy(), equal_nan=True), op
+
+
+# ------------------------------------------------------------- plus / mult
+
+BIOP_SHAPES = [((5,), (5,)), ((3, 4), (3, 1)), ((1,), (6, 2)), ((256, 1, 33), (256, 7, 1)),
+               ((4, 1, 3), (1, 5, 1)), ((0, 3), (0, 1)), ((), (4,)), ((1000, 100), (1000, 100))]
+
+
+@pytest.mark.parametrize("t", REAL_TYPES)
+@pytest.mark.parametrize("op", ["plus", "mult"])
+def test_biops_broadcast_exact(gpu, op, t):
+    rng = seeded(hash((op, t)) % 2**32)
+    for sa, sb in BIOP_SHAPES:
+        a, _ = rand_array(rng, t, sa[::-1])
+        b, _ = rand_array(rng, t, sb[::-1])
+        x, y = to_pdl(a, t), to_pdl(b, t)
+        for swap in (0, 1):
+            got = getattr(P, op)(x, y, swap=swap)
+            exp = O.run(op, [x, y], swap=swap)[0]
+            assert_same(got, exp, what=f"{op} {t} {sa}x{sb} swap={swap}")
+
+
+@pytest.mark.parametrize("t", ["float", "double", "long", "byte", "ulonglong"])
+@pytest.mark.parametrize("op", ["plus", "mult"])
+def test_biops_bad_values(gpu, op, t):
+    rng = seeded(13)
+    a, _ = rand_array(rng, t, (7, 50), bad_frac=0.1)
+    b, _ = rand_array(rng, t, (1, 50), bad_frac=0.1)
+    for fa, fb in [(1, 0), (0, 1), (1, 1)]:
+        x, y = to_pdl(a, t, fa), to_pdl(b, t, fb)
+        got = getattr(P, op)(x, y)
+        exp = O.run(op, [x, y])[0]
+        assert_same(got, exp, what=f"{op} {t} bad {fa}{fb}")
+
+
+def test_biop_mixed_types_promote(gpu):
+    x = P.pdl(np.array([1, 2, 250], np.uint8))
+    y = P.pdl(np.array([1.5, 2.5, 3.5], np.float32))
+    got, exp = P.plus(x, y), O.run("plus", [x, y])[0]
+    assert_same(got, exp, what="byte+float")
+    z = P.plus(x, x)  # byte arithmetic wraps
+    assert z.type == "byte" and list(z.numpy()) == [2, 4, 244]
+
+
+def test_biop_into_supplied_output_of_other_type(gpu):
+    x = P.pdl(np.arange(6, dtype=np.int32))
+    out = P.zeroes("double", 6)
+    r = P.plus(x, x, out)
+    assert r is out and list(out.numpy()) == [0, 2, 4, 6, 8, 10]
+
+
+# -------------------------------------------------------------------- inner
+
+@pytest.mark.parametrize("t", REAL_TYPES)
+def test_inner_all_types(gpu, t):
+    rng = seeded(hash(("inner", t)) % 2**32)
+    for sa, sb in [((7,), (7,)), ((33, 5), (33,)), ((1, 4), (9, 4)), ((0,), (0,)),
+                   ((3000, 6), (3000, 6)), ((20000,), (20000,))]:
+        a, _ = rand_array(rng, t, sa[::-1], -20, 20)
+        b, _ = rand_array(rng, t, sb[::-1], -20, 20)
+        x, y = to_pdl(a, t), to_pdl(b, t)
+        got, exp = P.inner(x, y), O.run("inner", [x, y])[0]
+        if t in FLOAT_TYPES:
+            n = max(sa[0], sb[0])
+            ab = np.abs(np.broadcast_to(a.astype(np.float64), np.broadcast_shapes(a.shape, b.shape)) *
+                        np.broadcast_to(b.astype(np.float64), np.broadcast_shapes(a.shape, b.shape)))
+            scale = ab.sum(axis=-1) + np.abs(exp.numpy())
+            assert_same(got, exp, rtol=(n + 2) * EPS[t], atol=1e-300, scale=scale, what=f"inner {t}")
+        else:
+            assert_same(got, exp, what=f"inner {t} {sa}")
+
+
+@pytest.mark.parametrize("t", ["double", "float", "long"])
+def test_inner_bad_and_views(gpu, t):
+    rng = seeded(17)
+    a, _ = rand_array(rng, t, (40, 64), -20, 20, bad_frac=0.01)
+    b, _ = rand_array(rng, t, (40, 64), -20, 20)
+    x, y = to_pdl(a, t, 1), to_pdl(b, t)
+    got, exp = P.inner(x, y), O.run("inner", [x, y])[0]
+    assert_same(got, exp, rtol=80 * EPS.get(t, 0), atol=1e-300,
+                scale=np.abs(a.astype(np.float64) * b).sum(-1) if t in FLOAT_TYPES else None,
+                what="inner bad")
+    xv = to_pdl(a, t).xchg(0, 1)
+    yv = to_pdl(b, t).xchg(0, 1)
+    got, exp = P.inner(xv, yv), O.run("inner", [xv, yv])[0]
+    assert_same(got, exp, rtol=80 * EPS.get(t, 0), atol=1e-300,
+                scale=np.abs(a.astype(np.float64) * b).sum(0) if t in FLOAT_TYPES else None,
+                what="inner views")
+
+
+# ------------------------------------------------------------------ matmult
+
+MM_SHAPES = [((3, 4), (2, 3)), ((5, 5), (5, 5)), ((1, 7), (7, 1)), ((130, 129), (131, 130)),
+             ((64, 200, 3), (150, 64)), ((17, 9, 2), (5, 17, 2)), ((8, 300), (260, 8))]
+
+
+@pytest.mark.parametrize("t", REAL_TYPES)
+def test_matmult_exact_all_types(gpu, t):
+    """The exact SIMT kernel keeps the reference's t order and rounding
+    (separately rounded product and sum): bit-identical for every type."""
+    rng = seeded(hash(("mm", t)) % 2**32)
+    P.set_matmult_mode(P.MATMULT_SIMT_EXACT)
+    try:
+        for sa, sb in MM_SHAPES:
+            a, _ = rand_array(rng, t, sa[::-1], -8, 8)
+            b, _ = rand_array(rng, t, sb[::-1], -8, 8)
+            x, y = to_pdl(a, t), to_pdl(b, t)
+            got, exp = P.matmult(x, y), O.run("matmult", [x, y])[0]
+            assert_same(got, exp, what=f"matmult {t} {sa}x{sb}")
+    finally:
+        P.set_matmult_mode(P.MATMULT_BF16X6)
+
+
+def test_matmult_float_with_bad_uses_exact_kernel(gpu):
+    rng = seeded(19)
+    # float32 with the badflag set runs the exact kernel in every mode
+    for sa, sb in MM_SHAPES:
+        a, _ = rand_array(rng, "float", sa[::-1], -8, 8)
+        b, _ = rand_array(rng, "float", sb[::-1], -8, 8)
+        x, y = to_pdl(a, "float", 1), to_pdl(b, "float")
+        got, exp = P.matmult(x, y), O.run("matmult", [x, y])[0]
+        assert_same(got, exp, what=f"matmult float exact {sa}x{sb}")
+
+
+@pytest.mark.parametrize("t", ["double", "float", "long"])
+def test_matmult_bad_values(gpu, t):
+    rng = seeded(23)
+    a, _ = rand_array(rng, t, (20, 30), -5, 5, bad_frac=0.01)
+    b, _ = rand_array(rng, t, (30, 25), -5, 5, bad_frac=0.01)
+    x, y = to_pdl(a, t, 1), to_pdl(b, t, 1)
+    got, exp = P.matmult(x, y), O.run("matmult", [x, y])[0]
+    assert_same(got, exp, what=f"matmult bad {t}")
+
+
+def test_matmult_simt_fp32_within_tolerance(gpu):
+    rng = seeded(29)
+    a = rng.standard_normal((300, 200)).astype(np.float32)
+    b = rng.standard_normal((200, 100)).astype(np.float32)
+    x, y = P.pdl(a), P.pdl(b)
+    P.set_matmult_mode(P.MATMULT_SIMT_FP32)
+    try:
+        got = P.matmult(x, y).numpy().astype(np.float64)
+    finally:
+        P.set_matmult_mode(P.MATMULT_BF16X6)
+    ref = a.astype(np.float64) @ b.astype(np.float64)
+    bound = (200 + 2) * EPS["float"] * (np.abs(a).astype(np.float64) @ np.abs(b))
+    assert np.all(np.abs(got - ref) <= bound)
+
+
+# ----------------------------------------------------- fused sumover(a*b+d)
+
+def test_fused_int32_outer_exact(gpu):
+    rng = seeded(31)
+    a, _ = rand_array(rng, "long", (40, 1, 96), -1000, 1000)   # numpy order of dims (96,1,40)
+    b, _ = rand_array(rng, "long", (1, 70, 96), -1000, 1000)
+    x, y = to_pdl(a, "long"), to_pdl(b, "long")
+    got = P.sumover_mult_plus(x, y, x)
+    t = O.run("mult", [x, y])[0]
+    u = O.run("plus", [t, x])[0]
+    exp = O.run("sumover", [u])[0]
+    assert_same(got, exp, what="fused int32")
+    assert "outer" in P.last_launch_info()["kernel"]
+
+
+@pytest.mark.parametrize("t", ["float", "double", "short", "ulong"])
+def test_fused_generic_and_bad(gpu, t):
+    rng = seeded(37)
+    for fa, fb, fd in [(0, 0, 0), (1, 0, 0), (1, 1, 1)]:
+        a, _ = rand_array(rng, t, (20, 1, 33), -50, 50, bad_frac=0.02 if fa else 0)
+        b, _ = rand_array(rng, t, (1, 9, 33), -50, 50, bad_frac=0.02 if fb else 0)
+        d, _ = rand_array(rng, t, (20, 1, 33), -50, 50, bad_frac=0.02 if fd else 0)
+        x, y, z = to_pdl(a, t, fa), to_pdl(b, t, fb), to_pdl(d, t, fd)
+        got = P.sumover_mult_plus(x, y, z)
+        tt = O.run("mult", [x, y])[0]
+        u = O.run("plus", [tt, z])[0]
+        exp = O.run("sumover", [u])[0]
+        scale = None
+        if t in FLOAT_TYPES:
+            un = np.abs(np.nan_to_num(u.numpy().astype(np.float64)))
+            un[u.numpy() == P.default_badvalue(type_code(t))] = 0
+            scale = un.sum(-1)
+        assert_same(got, exp, rtol=40 * EPS.get(t, 0), atol=1e-300, scale=scale,
+                    what=f"fused {t} {fa}{fb}{fd}")
+
+
+# ------------------------------------------------------------ conversions
+
+@pytest.mark.parametrize("src", REAL_TYPES)
+def test_convert_matches_c_casts(gpu, src):
+    rng = seeded(41)
+    a, _ = rand_array(rng, src, (3, 37), -100, 100)
+    x = to_pdl(a, src)
+    for dst in REAL_TYPES:
+        got = P.convert(x, dst).numpy()
+        if np.dtype(NP_DTYPES[type_code(dst)]).kind == "u" and a.dtype.kind == "f":
+            want = a.astype(np.int64).astype(NP_DTYPES[type_code(dst)])
+        else:
+            want = a.astype(NP_DTYPES[type_code(dst)])
+        assert np.array_equal(got, want), (src, dst)
