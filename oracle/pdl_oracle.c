@@ -280,9 +280,13 @@ typedef struct {
   int64_t inc_sizes[MAXP][2];
 } obrc;
 
-/* a dummy (broadcast) dim of a view: increment 0 */
+/* a dummy (broadcast) dim of a view: increment 0 (PDL tests the view's
+ * vafftrans increments; an empty ndarray is never a view of anything) */
 static int is_dummy(const pdlgb300_ndarray *p, int d) {
-  return d < p->ndims && p->incs[d] == 0;
+  if (d >= p->ndims || p->incs[d] != 0) return 0;
+  for (int i = 0; i < p->ndims; i++)
+    if (p->dims[i] == 0) return 0;
+  return 1;
 }
 
 static void default_incs(pdlgb300_ndarray *p) {

@@ -259,7 +259,15 @@ pdlgb300_error param_error(const pdlgb300_vtable *vt, int param, pdlgb300_ndarra
   return err(PDLGB300_EUSERERROR, "%s", m.c_str());
 }
 
-bool dummy_dim(const pdlgb300_ndarray *p, int d) { return d < p->ndims && p->incs[d] == 0; }
+// A dummy (broadcast) dim of a view has increment 0.  An empty ndarray's
+// default increments can be 0 too, and it holds nothing to write, so it is
+// never treated as a dummy.
+bool dummy_dim(const pdlgb300_ndarray *p, int d) {
+  if (d >= p->ndims || p->incs[d] != 0) return false;
+  for (int i = 0; i < p->ndims; i++)
+    if (p->dims[i] == 0) return false;
+  return true;
+}
 
 // Broadcast dims and increments, real-dim sizes, and the shapes of null
 // outputs (which get default increments).

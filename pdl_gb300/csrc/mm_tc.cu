@@ -1,10 +1,404 @@
-// mm_tc.cu -- float32 matmult as split-bf16 products on the tcgen05 tensor
-// cores (placeholder until the kernel lands: reports unsupported).
+// mm_tc.cu -- float32 matmult (lib/PDL/Primitive.pd:191-264) as split-bf16
+// products on the tcgen05 tensor cores with FP32 accumulation in TMEM.
+//
+// Split: every float32 x becomes bf16 limbs x0 = rn(x), x1 = rn(x - x0),
+// x2 = rn(x - x0 - x1) (each difference is exact in float32).  With three
+// limbs the six products a0b0 + a0b1 + a1b0 + a0b2 + a1b1 + a2b0 leave out
+// only terms below 2^-24 |a||b|, float32 territory; with two limbs the three
+// products a0b0 + a0b1 + a1b0 leave ~2^-16.  The split kernel writes the
+// limbs K-major (A: [limb][batch][h][t], B transposed: [limb][batch][w][t]),
+// t padded to a multiple of 32 with zeros.
+//
+// GEMM: one CTA (4 warps) per 128 (h) x 256 (w) output tile.  Warp 0 lane 0
+// streams K-slabs of 32 through a 3-4 stage ring with TMA (64-byte swizzle),
+// warp 1 lane 0 issues tcgen05.mma (M=128, N=256, K=16, bf16 in, f32
+// accumulate in 256 TMEM columns) for every limb product, and
+// tcgen05.commit releases each stage; after the last slab all four warps read
+// their 32 TMEM lanes (tcgen05.ld 32x32b) and store the tile.  Every
+// mbarrier wait gives up after ~4 s of clock64 time, records an error the
+// host reads back, and the CTA still frees its TMEM.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cudaTypedefs.h>
+
+#include <mutex>
+
 #include "args.cuh"
 
 namespace pg {
-bool matmult_tc_supported(const MMArgs &) { return false; }
-pdlgb300_error launch_matmult_tc(int, const MMArgs &, cudaStream_t) {
-  return pgh::err(PDLGB300_EFATAL, "tensor-core matmult not built");
+namespace {
+
+constexpr int TC_M = 128, TC_N = 256, TC_BK = 32;
+constexpr uint32_t A_TILE = TC_M * TC_BK * 2;  // 8 KiB
+constexpr uint32_t B_TILE = TC_N * TC_BK * 2;  // 16 KiB
+constexpr uint32_t TMEM_COLS = 256;
+constexpr long long WAIT_CYCLES = 8000000000LL;  // ~4 s at 2 GHz
+
+template <int LIMBS> struct TcCfg {
+  static constexpr int STAGES = LIMBS == 3 ? 3 : 4;
+  static constexpr int NPROD = LIMBS == 3 ? 6 : 3;
+  static constexpr uint32_t STAGE_BYTES = LIMBS * (A_TILE + B_TILE);
+  static constexpr uint32_t SMEM = STAGES * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
+};
+
+struct TcArgs {
+  char *c;
+  int64_t M, N, K, Kp;
+  int64_t c_n, c_m;
+  int64_t nA, nB;  // limb batches (1 when the operand is broadcast)
+  Loop L;          // batch loop: pdl 2 = c
+  int *err;
+};
+
+__device__ __forceinline__ uint32_t su32(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
 }
+__device__ __forceinline__ void mbar_init(uint64_t *b, uint32_t n) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(su32(b)), "r"(n) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *b, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(su32(b)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint64_t *b, uint32_t phase) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(su32(b)), "r"(phase)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait: false (and the error flag set) after WAIT_CYCLES.
+__device__ __forceinline__ bool mbar_wait(uint64_t *b, uint32_t phase, int *err) {
+  if (mbar_try(b, phase)) return true;
+  const long long t0 = clock64();
+  while (!mbar_try(b, phase)) {
+    if (clock64() - t0 > WAIT_CYCLES) {
+      atomicExch(err, 1);
+      return false;
+    }
+  }
+  return true;
+}
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, uint64_t *bar,
+                                            int x, int y) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%3, %4}], [%2];" ::"r"(su32(dst)),
+      "l"((uint64_t)map), "r"(su32(bar)), "r"(x), "r"(y)
+      : "memory");
+}
+// Shared-memory matrix descriptor, K-major, 64-byte swizzle: rows of 64 B,
+// 8-row groups 512 B apart (SBO), descriptor version 1, layout SWIZZLE_64B.
+__device__ __forceinline__ uint64_t sdesc_sw64(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)1 << 16;            // leading byte offset (unused here)
+  d |= (uint64_t)(512 >> 4) << 32;   // stride byte offset
+  d |= (uint64_t)1 << 46;            // version
+  d |= (uint64_t)4 << 61;            // SWIZZLE_64B
+  return d;
+}
+// Instruction descriptor: kind::f16, A/B bf16, D f32, both K-major.
+constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TC_N >> 3) << 17) |
+                           ((uint32_t)(TC_M >> 4) << 24);
+
+__device__ __forceinline__ void umma(uint32_t tmem, uint64_t a, uint64_t b, uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
+      "l"(a), "l"(b), "r"(IDESC), "r"(acc)
+      : "memory");
+}
+__device__ __forceinline__ void umma_commit(uint64_t *bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          su32(bar))
+      : "memory");
+}
+
+template <int LIMBS>
+__global__ void __launch_bounds__(128, 1)
+    k_mm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+            const TcArgs g) {
+  using C = TcCfg<LIMBS>;
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t *base = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t *full = (uint64_t *)(base + C::STAGES * C::STAGE_BYTES);
+  uint64_t *empty = full + C::STAGES;
+  uint64_t *done = empty + C::STAGES;
+  uint32_t *tmem_slot = (uint32_t *)(done + 1);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     su32(tmem_slot)),
+                 "r"(TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (threadIdx.x == 32) {
+    for (int s = 0; s < C::STAGES; s++) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(done, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+
+  const int z = blockIdx.z;
+  const int nk = (int)(g.Kp / TC_BK);
+  const int64_t m0 = (int64_t)blockIdx.y * TC_M, n0 = (int64_t)blockIdx.x * TC_N;
+  // limb products (a limb, b limb): the large one first
+  constexpr int PA[6] = {0, 0, 1, 0, 1, 2};
+  constexpr int PB[6] = {0, 1, 0, 2, 1, 0};
+  bool ok = true;
+
+  if (warp == 0 && lane == 0) {
+    // ---------------------------------------------------------- producer
+    const int za = g.nA == 1 ? 0 : z, zb = g.nB == 1 ? 0 : z;
+    for (int kb = 0; kb < nk && ok; kb++) {
+      const int s = kb % C::STAGES, use = kb / C::STAGES;
+      if (use > 0) ok = mbar_wait(&empty[s], (use - 1) & 1, g.err);
+      if (!ok) break;
+      uint8_t *st = base + s * C::STAGE_BYTES;
+      mbar_expect_tx(&full[s], C::STAGE_BYTES);
+#pragma unroll
+      for (int l = 0; l < LIMBS; l++)
+        tma_load_2d(st + l * A_TILE, &tmA, &full[s], kb * TC_BK,
+                    (int)((l * g.nA + za) * g.M + m0));
+#pragma unroll
+      for (int l = 0; l < LIMBS; l++)
+        tma_load_2d(st + LIMBS * A_TILE + l * B_TILE, &tmB, &full[s], kb * TC_BK,
+                    (int)((l * g.nB + zb) * g.N + n0));
+    }
+  } else if (warp == 1 && lane == 0) {
+    // ------------------------------------------------------------ MMA
+    for (int kb = 0; kb < nk && ok; kb++) {
+      const int s = kb % C::STAGES, use = kb / C::STAGES;
+      ok = mbar_wait(&full[s], use & 1, g.err);
+      if (!ok) break;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t st = su32(base + s * C::STAGE_BYTES);
+#pragma unroll
+      for (int ks = 0; ks < TC_BK / 16; ks++) {
+#pragma unroll
+        for (int p = 0; p < C::NPROD; p++) {
+          const uint64_t ad = sdesc_sw64(st + PA[p] * A_TILE + ks * 32);
+          const uint64_t bd = sdesc_sw64(st + LIMBS * A_TILE + PB[p] * B_TILE + ks * 32);
+          umma(tmem, ad, bd, (kb | ks | p) != 0);
+        }
+      }
+      umma_commit(&empty[s]);
+    }
+    umma_commit(done);
+  }
+  __syncwarp();
+
+  // -------------------------------------------------------------- epilogue
+  ok = mbar_wait(done, 0, g.err);
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (ok) {
+    int64_t offs[MAXP];
+    loop_offsets(g.L, z, offs);
+    float *C0 = reinterpret_cast<float *>(g.c) + offs[2];
+    const int64_t m = m0 + warp * 32 + lane;
+    const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
+    const bool vec = g.c_n == 1 && ((uintptr_t)C0 % 16 == 0) && (g.c_m % 4 == 0);
+#pragma unroll 1
+    for (int c0 = 0; c0 < TC_N; c0 += 16) {
+      uint32_t r[16];
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+          "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
+            "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]),
+            "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+          : "r"(trow + (uint32_t)c0));
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      if (m < g.M) {
+        const int64_t n = n0 + c0;
+        float *row = C0 + m * g.c_m;
+        if (vec && n + 16 <= g.N) {
+          float4 *p = reinterpret_cast<float4 *>(row + n);
+#pragma unroll
+          for (int q = 0; q < 4; q++)
+            p[q] = make_float4(__uint_as_float(r[4 * q]), __uint_as_float(r[4 * q + 1]),
+                               __uint_as_float(r[4 * q + 2]), __uint_as_float(r[4 * q + 3]));
+        } else {
+#pragma unroll
+          for (int j = 0; j < 16; j++)
+            if (n + j < g.N) row[(n + j) * g.c_n] = __uint_as_float(r[j]);
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(TMEM_COLS)
+                 : "memory");
+}
+
+// ------------------------------------------------------------------ split
+
+struct SplitArgs {
+  const float *src;
+  __nv_bfloat16 *dst;    // [LIMBS][nb][rows][Kp]
+  int64_t rows, K, Kp, nb;
+  int64_t s_row, s_k;    // element increments of a row / of k in src
+  Loop L;                // batch loop (pdl index `p`)
+  int p;
+};
+
+template <int LIMBS>
+__global__ void __launch_bounds__(256) k_split(const SplitArgs g) {
+  const int64_t per = g.rows * g.Kp, total = per * g.nb;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t z = i / per, r = (i - z * per) / g.Kp, k = i % g.Kp;
+    float x = 0.f;
+    if (k < g.K) {
+      int64_t offs[MAXP];
+      loop_offsets(g.L, z, offs);
+      x = g.src[offs[g.p] + r * g.s_row + k * g.s_k];
+    }
+    __nv_bfloat16 h0 = __float2bfloat16_rn(x);
+    float r1 = __fsub_rn(x, __bfloat162float(h0));
+    __nv_bfloat16 h1 = __float2bfloat16_rn(r1);
+    g.dst[i] = h0;
+    g.dst[total + i] = h1;
+    if (LIMBS == 3) {
+      float r2 = __fsub_rn(r1, __bfloat162float(h1));
+      g.dst[2 * total + i] = __float2bfloat16_rn(r2);
+    }
+  }
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+std::once_flag g_encode_once;
+
+bool get_encode() {
+  std::call_once(g_encode_once, [] {
+    void *fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      g_encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+  });
+  return g_encode != nullptr;
+}
+
+bool make_map(CUtensorMap *map, void *ptr, int64_t kp, int64_t rows, uint32_t boxrows) {
+  cuuint64_t gdim[2] = {(cuuint64_t)kp, (cuuint64_t)rows};
+  cuuint64_t gstride[1] = {(cuuint64_t)kp * 2};
+  cuuint32_t box[2] = {(cuuint32_t)TC_BK, boxrows};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = g_encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, ptr, gdim, gstride, box, estr,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
+                        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
+bool all_zero_incs(const Loop &L, int p) {
+  for (int k = 0; k < L.nd; k++)
+    if (L.size[k] > 1 && L.inc[p][k] != 0) return false;
+  return true;
+}
+
+template <int LIMBS>
+pdlgb300_error tc_typed(const MMArgs &g, cudaStream_t s) {
+  using C = TcCfg<LIMBS>;
+  pdlgb300_error e = pgh::ok();
+  if (!get_encode()) return pgh::err(PDLGB300_EFATAL, "cuTensorMapEncodeTiled unavailable");
+  const int64_t Kp = (g.K + TC_BK - 1) / TC_BK * TC_BK;
+  const int64_t nA = all_zero_incs(g.L, 0) ? 1 : g.batch;
+  const int64_t nB = all_zero_incs(g.L, 1) ? 1 : g.batch;
+  const size_t abytes = (size_t)LIMBS * nA * g.M * Kp * 2, bbytes = (size_t)LIMBS * nB * g.N * Kp * 2;
+  void *scratch = nullptr;
+  if (cudaMallocAsync(&scratch, abytes + bbytes + 256 + 16, s) != cudaSuccess) {
+    cudaGetLastError();
+    return pgh::err(PDLGB300_EFATAL, "matmult: no device memory for the bf16 limbs");
+  }
+  __nv_bfloat16 *al = (__nv_bfloat16 *)scratch;
+  __nv_bfloat16 *bl = (__nv_bfloat16 *)((char *)scratch + ((abytes + 255) & ~(size_t)255));
+  int *errp = (int *)((char *)bl + bbytes);
+  errp = (int *)(((uintptr_t)errp + 15) & ~(uintptr_t)15);
+  cudaMemsetAsync(errp, 0, sizeof(int), s);
+  const int nsm = pgh::num_sms();
+  SplitArgs sa{reinterpret_cast<const float *>(g.a), al, g.M, g.K, Kp, nA, g.a_m, g.a_k, g.L, 0};
+  int64_t ga = std::min<int64_t>((nA * g.M * Kp + 255) / 256, (int64_t)nsm * 32);
+  k_split<LIMBS><<<(int)ga, 256, 0, s>>>(sa);
+  SplitArgs sb{reinterpret_cast<const float *>(g.b), bl, g.N, g.K, Kp, nB, g.b_n, g.b_k, g.L, 1};
+  int64_t gb = std::min<int64_t>((nB * g.N * Kp + 255) / 256, (int64_t)nsm * 32);
+  k_split<LIMBS><<<(int)gb, 256, 0, s>>>(sb);
+  if (!pgh::cuda_check(cudaGetLastError(), &e, "k_split")) {
+    cudaFreeAsync(scratch, s);
+    return e;
+  }
+  pgh::record_kernel("k_split", ga, 256);
+  CUtensorMap mA, mB;
+  if (!make_map(&mA, al, Kp, LIMBS * nA * g.M, TC_M) ||
+      !make_map(&mB, bl, Kp, LIMBS * nB * g.N, TC_N)) {
+    cudaFreeAsync(scratch, s);
+    return pgh::err(PDLGB300_EFATAL, "matmult: tensor map encoding failed");
+  }
+  TcArgs t;
+  memset(&t, 0, sizeof t);
+  t.c = g.c;
+  t.M = g.M;
+  t.N = g.N;
+  t.K = g.K;
+  t.Kp = Kp;
+  t.c_n = g.c_n;
+  t.c_m = g.c_m;
+  t.nA = nA;
+  t.nB = nB;
+  t.L = g.L;
+  t.err = errp;
+  static bool attr_set[4] = {false, false, false, false};
+  if (!attr_set[LIMBS]) {
+    cudaFuncSetAttribute(k_mm_tc<LIMBS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::SMEM);
+    attr_set[LIMBS] = true;
+  }
+  dim3 grid((unsigned)((g.N + TC_N - 1) / TC_N), (unsigned)((g.M + TC_M - 1) / TC_M),
+            (unsigned)g.batch);
+  k_mm_tc<LIMBS><<<grid, 128, C::SMEM, s>>>(mA, mB, t);
+  if (!pgh::cuda_check(cudaGetLastError(), &e, "k_mm_tc")) {
+    cudaFreeAsync(scratch, s);
+    return e;
+  }
+  pgh::record_kernel(LIMBS == 3 ? "k_mm_tc_bf16x6" : "k_mm_tc_bf16x3",
+                     (int64_t)grid.x * grid.y * grid.z, 128);
+  int herr = 0;
+  cudaMemcpyAsync(&herr, errp, sizeof(int), cudaMemcpyDeviceToHost, s);
+  cudaFreeAsync(scratch, s);
+  cudaError_t ce = cudaStreamSynchronize(s);
+  if (ce != cudaSuccess) return pgh::err(PDLGB300_EFATAL, "matmult: %s", cudaGetErrorString(ce));
+  if (herr) return pgh::err(PDLGB300_EFATAL, "matmult: tensor-core pipeline wait timed out");
+  return e;
+}
+
+}  // namespace
+
+bool matmult_tc_supported(const MMArgs &g) {
+  return g.M > 0 && g.N > 0 && g.K > 0 && g.batch > 0 && g.batch <= 65535 &&
+         !g.bad && g.M * (3 * g.batch) < (1LL << 31) && g.N * (3 * g.batch) < (1LL << 31) &&
+         g.K < (1LL << 31);
+}
+
+pdlgb300_error launch_matmult_tc(int limbs, const MMArgs &g, cudaStream_t s) {
+  return limbs == 3 ? tc_typed<3>(g, s) : tc_typed<2>(g, s);
+}
+
 }  // namespace pg

@@ -85,8 +85,9 @@ template <class In, class Out, bool COMP> struct OpSum {
   static constexpr bool kCount = false, kVec = true;
   static constexpr bool kBlock = std::is_same_v<Acc, F64Sum>;
   static constexpr int kU = kBlock ? 8 : 0;
-  template <int B> __device__ static void add_block(Acc &a, const In *v) {
-    if constexpr (kBlock) a.template add_block<B>(v);
+  template <int VEC, int U>
+  __device__ static void add_block(Acc &a, const In *v, int64_t, int64_t) {
+    if constexpr (kBlock) a.template add_block<VEC * U>(v);
   }
   __device__ static Acc init() { return S::init(); }
   __device__ static void add(Acc &a, In v, int64_t) { S::add(a, v); }
@@ -108,7 +109,8 @@ template <class In, class Out> struct OpProd {
   using Acc = std::conditional_t<std::is_integral_v<Out>, uns_t<Out>, Out>;
   static constexpr bool kCount = false, kVec = true, kBlock = false;
   static constexpr int kU = 0;
-  template <int B> __device__ static void add_block(Acc &, const In *) {}
+  template <int VEC, int U>
+  __device__ static void add_block(Acc &, const In *, int64_t, int64_t) {}
   __device__ static Acc init() { return (Acc)1; }
   __device__ static void add(Acc &a, In v, int64_t) {
     if constexpr (std::is_integral_v<Out>) a = (Acc)wmul<Out>((Out)a, (Out)v);
@@ -134,8 +136,9 @@ template <class In, class Out, bool COMP> struct OpAvg {
   static constexpr bool kCount = true, kVec = true;
   static constexpr bool kBlock = std::is_same_v<Acc, F64Sum>;
   static constexpr int kU = kBlock ? 8 : 0;
-  template <int B> __device__ static void add_block(Acc &a, const In *v) {
-    if constexpr (kBlock) a.template add_block<B>(v);
+  template <int VEC, int U>
+  __device__ static void add_block(Acc &a, const In *v, int64_t, int64_t) {
+    if constexpr (kBlock) a.template add_block<VEC * U>(v);
   }
   __device__ static Acc init() { return S::init(); }
   __device__ static void add(Acc &a, In v, int64_t) { S::add(a, v); }
@@ -177,7 +180,8 @@ template <class T, bool MAX, bool IND> struct OpMM {
   using Out = std::conditional_t<IND, int64_t, T>;
   static constexpr bool kCount = false, kVec = true, kBlock = false;
   static constexpr int kU = 0;
-  template <int B> __device__ static void add_block(Acc &, const T *) {}
+  template <int VEC, int U>
+  __device__ static void add_block(Acc &, const T *, int64_t, int64_t) {}
   __device__ static Acc init() { return Acc{-1, (T)0}; }
   __device__ static bool better(T x, int64_t ix, T y, int64_t iy) {
     // does (x, ix) replace (y, iy)?  (ix > iy in sequential order)
@@ -204,6 +208,102 @@ template <class T, bool MAX, bool IND> struct OpMM {
       return badval;
     }
     if constexpr (IND) return a.idx; else return a.v;
+  }
+};
+
+// float64 minimum/maximum(+_ind) on the integer pipe.  GB300 retires about
+// 1.6 FP64 instructions per clock per SM, so FP64 compares cannot keep up
+// with HBM; instead each double maps to an ordered int64 key (sign-magnitude
+// to two's complement: monotonic, -0 == +0) and a 16-element block is
+// settled by an integer tournament in index order.  Blocks holding an inf
+// or NaN take the exact per-element rule.  In key space (maximum negates
+// the key) NaN is the worst key; equal keys go to the lower index, except
+// NaN against NaN, which goes to the higher index.
+__device__ __forceinline__ int64_t dkey(uint64_t b) {
+  int64_t mag = (int64_t)(b & 0x7FFFFFFFFFFFFFFFull);
+  int64_t s = (int64_t)b >> 63;
+  return (mag ^ s) - s;
+}
+constexpr int64_t KEY_NAN = 0x7FFFFFFFFFFFFFFFll;
+
+template <bool MAX, bool IND> struct OpMM<double, MAX, IND> {
+  struct Acc {
+    int64_t key;
+    int64_t idx;  // -1: empty
+    uint64_t bits;
+  };
+  using Out = std::conditional_t<IND, int64_t, double>;
+  static constexpr bool kCount = false, kVec = true, kBlock = true;
+  static constexpr int kU = 8;
+  __device__ static int64_t key_of(uint64_t b) {
+    if ((b & 0x7FFFFFFFFFFFFFFFull) > 0x7FF0000000000000ull) return KEY_NAN;
+    int64_t k = dkey(b);
+    return MAX ? -k : k;
+  }
+  __device__ static bool better(int64_t k, int64_t i, int64_t k2, int64_t i2) {
+    return k < k2 || (k == k2 && (k == KEY_NAN ? i > i2 : i < i2));
+  }
+  __device__ static Acc init() { return Acc{KEY_NAN, -1, 0}; }
+  __device__ static void add(Acc &a, double v, int64_t i) {
+    uint64_t b = (uint64_t)__double_as_longlong(v);
+    int64_t k = key_of(b);
+    if (a.idx < 0 || better(k, i, a.key, a.idx)) a = Acc{k, i, b};
+  }
+  template <int VEC> __device__ static void add_vec(Acc &a, const double *v, int64_t i) {
+#pragma unroll
+    for (int e = 0; e < VEC; e++) add(a, v[e], i + e);
+  }
+  template <int VEC, int U>
+  __device__ static void add_block(Acc &a, const double *v, int64_t base, int64_t ustride) {
+    constexpr int B = VEC * U;
+    const uint64_t *bits = reinterpret_cast<const uint64_t *>(v);
+    int64_t k[B];
+    uint64_t w[B];
+    int p[B];
+    uint32_t special = 0;
+#pragma unroll
+    for (int j = 0; j < B; j++) {
+      uint32_t hi = (uint32_t)(bits[j] >> 32);
+      special |= (~hi & 0x7FF00000u) == 0;  // exponent all ones: inf or NaN
+      int64_t kk = dkey(bits[j]);
+      k[j] = MAX ? -kk : kk;
+      w[j] = bits[j];
+      p[j] = j;
+    }
+    if (special) {
+#pragma unroll
+      for (int j = 0; j < B; j++)
+        add(a, v[j], base + (j / VEC) * ustride + (j % VEC));
+      return;
+    }
+    // tournament in index order: the right (later) side wins only if smaller
+#pragma unroll
+    for (int s = 1; s < B; s <<= 1) {
+#pragma unroll
+      for (int j = 0; j < B; j += 2 * s) {
+        bool r = k[j + s] < k[j];
+        k[j] = r ? k[j + s] : k[j];
+        p[j] = r ? p[j + s] : p[j];
+        if constexpr (!IND) w[j] = r ? w[j + s] : w[j];
+      }
+    }
+    if (a.idx < 0 || k[0] < a.key) {
+      a.key = k[0];
+      a.idx = base + (p[0] / VEC) * ustride + (p[0] % VEC);
+      a.bits = IND ? 0 : w[0];
+    }
+  }
+  __device__ static void merge(Acc &a, const Acc &b) {
+    if (b.idx < 0) return;
+    if (a.idx < 0 || better(b.key, b.idx, a.key, a.idx)) a = b;
+  }
+  __device__ static Out fin(const Acc &a, int64_t, bool, Out badval, int *setbad) {
+    if (a.idx < 0) {
+      *setbad = 1;
+      return badval;
+    }
+    if constexpr (IND) return a.idx;
+    else return __longlong_as_double((long long)a.bits);
   }
 };
 
@@ -299,7 +399,8 @@ __device__ __forceinline__ void row_accumulate(const In *row, int64_t lo, int64_
     }
     if constexpr (!BAD && Op::kBlock) {
       if (full) {
-        Op::template add_block<VEC * U>(ac.acc, reinterpret_cast<const In *>(buf));
+        Op::template add_block<VEC, U>(ac.acc, reinterpret_cast<const In *>(buf),
+                                       i + k * VEC, (int64_t)G * VEC);
         if constexpr (Op::kCount) ac.cnt += VEC * U;
         continue;
       }
