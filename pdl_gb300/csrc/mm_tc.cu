@@ -9,14 +9,19 @@
 // limbs K-major (A: [limb][batch][h][t], B transposed: [limb][batch][w][t]),
 // t padded to a multiple of 32 with zeros.
 //
-// GEMM: one CTA (4 warps) per 128 (h) x 256 (w) output tile.  Warp 0 lane 0
-// streams K-slabs of 32 through a 3-4 stage ring with TMA (64-byte swizzle),
-// warp 1 lane 0 issues tcgen05.mma (M=128, N=256, K=16, bf16 in, f32
-// accumulate in 256 TMEM columns) for every limb product, and
-// tcgen05.commit releases each stage; after the last slab all four warps read
-// their 32 TMEM lanes (tcgen05.ld 32x32b) and store the tile.  Every
-// mbarrier wait gives up after ~4 s of clock64 time, records an error the
-// host reads back, and the CTA still frees its TMEM.
+// GEMM: one CTA (10 warps) per 128 (h) x 256 (w) output tile.  Warp 8
+// streams K-slabs of 32 through a 3-4 stage ring with TMA (64-byte swizzle);
+// warp 9 issues tcgen05.mma (M=128, N=256, K=16, bf16 in, f32 accumulate)
+// for every limb product of a slab into one of two 256-column TMEM buffers,
+// starting the buffer fresh and adding the small limb products before the
+// large a0*b0 ones.  The tensor core's float32 accumulation truncates, so
+// long accumulation chains in TMEM drift toward zero (about 8e-6 normwise at
+// K=1024); instead warps 0-7 drain each finished slab buffer (tcgen05.ld
+// 32x32b, each warp its 32 lanes and half of the columns) into registers
+// with round-to-nearest adds while the next slab runs in the other buffer,
+// and finally store the tile.  Every mbarrier wait gives up after ~4 s of
+// clock64 time, records an error the host reads back, and the CTA still
+// frees its TMEM.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cudaTypedefs.h>
@@ -31,7 +36,7 @@ namespace {
 constexpr int TC_M = 128, TC_N = 256, TC_BK = 32;
 constexpr uint32_t A_TILE = TC_M * TC_BK * 2;  // 8 KiB
 constexpr uint32_t B_TILE = TC_N * TC_BK * 2;  // 16 KiB
-constexpr uint32_t TMEM_COLS = 256;
+constexpr uint32_t TMEM_COLS = 512;  // two 256-column slab accumulators
 constexpr long long WAIT_CYCLES = 8000000000LL;  // ~4 s at 2 GHz
 
 template <int LIMBS> struct TcCfg {
@@ -122,7 +127,7 @@ __device__ __forceinline__ void umma_commit(uint64_t *bar) {
 }
 
 template <int LIMBS>
-__global__ void __launch_bounds__(128, 1)
+__global__ void __launch_bounds__(320, 1)
     k_mm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
             const TcArgs g) {
   using C = TcCfg<LIMBS>;
@@ -130,23 +135,27 @@ __global__ void __launch_bounds__(128, 1)
   uint8_t *base = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint64_t *full = (uint64_t *)(base + C::STAGES * C::STAGE_BYTES);
   uint64_t *empty = full + C::STAGES;
-  uint64_t *done = empty + C::STAGES;
-  uint32_t *tmem_slot = (uint32_t *)(done + 1);
+  uint64_t *accf = empty + C::STAGES;  // slab accumulated in TMEM buffer b
+  uint64_t *acce = accf + 2;           // TMEM buffer b drained by the 8 accumulator warps
+  uint32_t *tmem_slot = (uint32_t *)(acce + 2);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
-  if (warp == 0) {
+  if (warp == 8) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      su32(tmem_slot)),
                  "r"(TMEM_COLS)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
-  if (threadIdx.x == 32) {
+  if (threadIdx.x == 288) {
     for (int s = 0; s < C::STAGES; s++) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
-    mbar_init(done, 1);
+    for (int b = 0; b < 2; b++) {
+      mbar_init(&accf[b], 1);
+      mbar_init(&acce[b], 8);
+    }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -157,93 +166,123 @@ __global__ void __launch_bounds__(128, 1)
   const int z = blockIdx.z;
   const int nk = (int)(g.Kp / TC_BK);
   const int64_t m0 = (int64_t)blockIdx.y * TC_M, n0 = (int64_t)blockIdx.x * TC_N;
-  // limb products (a limb, b limb): the large one first
-  constexpr int PA[6] = {0, 0, 1, 0, 1, 2};
-  constexpr int PB[6] = {0, 1, 0, 2, 1, 0};
+  // limb products (a limb, b limb), smallest first: each slab starts a fresh
+  // accumulator, so only the last (a0 b0) products are added at full size
+  constexpr int PA3[6] = {2, 1, 0, 1, 0, 0}, PB3[6] = {0, 1, 2, 0, 1, 0};
+  constexpr int PA2[3] = {1, 0, 0}, PB2[3] = {0, 1, 0};
   bool ok = true;
 
-  if (warp == 0 && lane == 0) {
-    // ---------------------------------------------------------- producer
-    const int za = g.nA == 1 ? 0 : z, zb = g.nB == 1 ? 0 : z;
-    for (int kb = 0; kb < nk && ok; kb++) {
-      const int s = kb % C::STAGES, use = kb / C::STAGES;
-      if (use > 0) ok = mbar_wait(&empty[s], (use - 1) & 1, g.err);
-      if (!ok) break;
-      uint8_t *st = base + s * C::STAGE_BYTES;
-      mbar_expect_tx(&full[s], C::STAGE_BYTES);
+  if (warp == 8) {
+    if (lane == 0) {
+      // -------------------------------------------------------- producer
+      const int za = g.nA == 1 ? 0 : z, zb = g.nB == 1 ? 0 : z;
+      for (int kb = 0; kb < nk && ok; kb++) {
+        const int s = kb % C::STAGES, use = kb / C::STAGES;
+        if (use > 0) ok = mbar_wait(&empty[s], (use - 1) & 1, g.err);
+        if (!ok) break;
+        uint8_t *st = base + s * C::STAGE_BYTES;
+        mbar_expect_tx(&full[s], C::STAGE_BYTES);
 #pragma unroll
-      for (int l = 0; l < LIMBS; l++)
-        tma_load_2d(st + l * A_TILE, &tmA, &full[s], kb * TC_BK,
-                    (int)((l * g.nA + za) * g.M + m0));
+        for (int l = 0; l < LIMBS; l++)
+          tma_load_2d(st + l * A_TILE, &tmA, &full[s], kb * TC_BK,
+                      (int)((l * g.nA + za) * g.M + m0));
 #pragma unroll
-      for (int l = 0; l < LIMBS; l++)
-        tma_load_2d(st + LIMBS * A_TILE + l * B_TILE, &tmB, &full[s], kb * TC_BK,
-                    (int)((l * g.nB + zb) * g.N + n0));
+        for (int l = 0; l < LIMBS; l++)
+          tma_load_2d(st + LIMBS * A_TILE + l * B_TILE, &tmB, &full[s], kb * TC_BK,
+                      (int)((l * g.nB + zb) * g.N + n0));
+      }
     }
-  } else if (warp == 1 && lane == 0) {
-    // ------------------------------------------------------------ MMA
-    for (int kb = 0; kb < nk && ok; kb++) {
-      const int s = kb % C::STAGES, use = kb / C::STAGES;
-      ok = mbar_wait(&full[s], use & 1, g.err);
-      if (!ok) break;
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint32_t st = su32(base + s * C::STAGE_BYTES);
-#pragma unroll
-      for (int ks = 0; ks < TC_BK / 16; ks++) {
+  } else if (warp == 9) {
+    if (lane == 0) {
+      // ------------------------------------------------------------- MMA
+      for (int kb = 0; kb < nk && ok; kb++) {
+        const int s = kb % C::STAGES, use = kb / C::STAGES;
+        const int b = kb & 1, j = kb >> 1;
+        if (j > 0) ok = mbar_wait(&acce[b], (j - 1) & 1, g.err);
+        if (ok) ok = mbar_wait(&full[s], use & 1, g.err);
+        if (!ok) break;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t st = su32(base + s * C::STAGE_BYTES);
+        const uint32_t d = tmem + (uint32_t)(b * TC_N);
+        int first = 1;
 #pragma unroll
         for (int p = 0; p < C::NPROD; p++) {
-          const uint64_t ad = sdesc_sw64(st + PA[p] * A_TILE + ks * 32);
-          const uint64_t bd = sdesc_sw64(st + LIMBS * A_TILE + PB[p] * B_TILE + ks * 32);
-          umma(tmem, ad, bd, (kb | ks | p) != 0);
-        }
-      }
-      umma_commit(&empty[s]);
-    }
-    umma_commit(done);
-  }
-  __syncwarp();
-
-  // -------------------------------------------------------------- epilogue
-  ok = mbar_wait(done, 0, g.err);
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  if (ok) {
-    int64_t offs[MAXP];
-    loop_offsets(g.L, z, offs);
-    float *C0 = reinterpret_cast<float *>(g.c) + offs[2];
-    const int64_t m = m0 + warp * 32 + lane;
-    const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
-    const bool vec = g.c_n == 1 && ((uintptr_t)C0 % 16 == 0) && (g.c_m % 4 == 0);
-#pragma unroll 1
-    for (int c0 = 0; c0 < TC_N; c0 += 16) {
-      uint32_t r[16];
-      asm volatile(
-          "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
-          "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
-            "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]),
-            "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-          : "r"(trow + (uint32_t)c0));
-      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-      if (m < g.M) {
-        const int64_t n = n0 + c0;
-        float *row = C0 + m * g.c_m;
-        if (vec && n + 16 <= g.N) {
-          float4 *p = reinterpret_cast<float4 *>(row + n);
 #pragma unroll
-          for (int q = 0; q < 4; q++)
-            p[q] = make_float4(__uint_as_float(r[4 * q]), __uint_as_float(r[4 * q + 1]),
-                               __uint_as_float(r[4 * q + 2]), __uint_as_float(r[4 * q + 3]));
+          for (int ks = 0; ks < TC_BK / 16; ks++) {
+            const int pa = LIMBS == 3 ? PA3[p] : PA2[p], pb = LIMBS == 3 ? PB3[p] : PB2[p];
+            const uint64_t ad = sdesc_sw64(st + pa * A_TILE + ks * 32);
+            const uint64_t bd = sdesc_sw64(st + LIMBS * A_TILE + pb * B_TILE + ks * 32);
+            umma(d, ad, bd, first ? 0u : 1u);
+            first = 0;
+          }
+        }
+        umma_commit(&empty[s]);
+        umma_commit(&accf[b]);
+      }
+    }
+  } else {
+    // ------------------------------------------- accumulators (warps 0-7)
+    // warp w reads TMEM lanes 32*(w%4).. (its 32 rows) and columns
+    // 128*(w/4).. (its half of the tile), adding each slab with RN fp32.
+    const int q = warp & 3, half = warp >> 2;
+    float acc[128];
+#pragma unroll
+    for (int i = 0; i < 128; i++) acc[i] = 0.f;
+    const uint32_t tl = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(half * 128);
+    for (int kb = 0; kb < nk && ok; kb++) {
+      const int b = kb & 1;
+      if (lane == 0) ok = mbar_wait(&accf[b], (kb >> 1) & 1, g.err);
+      ok = __shfl_sync(0xffffffffu, ok, 0);  // warp-uniform for tcgen05.ld
+      if (!ok) break;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+      for (int c = 0; c < 4; c++) {
+        uint32_t r[32];
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+            "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+            "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
+              "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]),
+              "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]),
+              "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+              "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]),
+              "=r"(r[30]), "=r"(r[31])
+            : "r"(tl + (uint32_t)(b * TC_N + c * 32)));
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+        for (int i = 0; i < 32; i++) acc[c * 32 + i] = __fadd_rn(acc[c * 32 + i], __uint_as_float(r[i]));
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncwarp();
+      if (lane == 0)
+        asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(&acce[b])) : "memory");
+    }
+    if (ok) {
+      int64_t offs[MAXP];
+      loop_offsets(g.L, z, offs);
+      float *C0 = reinterpret_cast<float *>(g.c) + offs[2];
+      const int64_t m = m0 + q * 32 + lane;
+      const int64_t nb = n0 + half * 128;
+      const bool vec = g.c_n == 1 && ((uintptr_t)C0 % 16 == 0) && (g.c_m % 4 == 0);
+      if (m < g.M) {
+        float *row = C0 + m * g.c_m;
+        if (vec && nb + 128 <= g.N) {
+          float4 *p = reinterpret_cast<float4 *>(row + nb);
+#pragma unroll
+          for (int i = 0; i < 32; i++)
+            p[i] = make_float4(acc[4 * i], acc[4 * i + 1], acc[4 * i + 2], acc[4 * i + 3]);
         } else {
 #pragma unroll
-          for (int j = 0; j < 16; j++)
-            if (n + j < g.N) row[(n + j) * g.c_n] = __uint_as_float(r[j]);
+          for (int i = 0; i < 128; i++)
+            if (nb + i < g.N) row[(nb + i) * g.c_n] = acc[i];
         }
       }
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
-  if (warp == 0)
+  if (warp == 8)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
                  "r"(TMEM_COLS)
                  : "memory");
@@ -373,13 +412,13 @@ pdlgb300_error tc_typed(const MMArgs &g, cudaStream_t s) {
   }
   dim3 grid((unsigned)((g.N + TC_N - 1) / TC_N), (unsigned)((g.M + TC_M - 1) / TC_M),
             (unsigned)g.batch);
-  k_mm_tc<LIMBS><<<grid, 128, C::SMEM, s>>>(mA, mB, t);
+  k_mm_tc<LIMBS><<<grid, 320, C::SMEM, s>>>(mA, mB, t);
   if (!pgh::cuda_check(cudaGetLastError(), &e, "k_mm_tc")) {
     cudaFreeAsync(scratch, s);
     return e;
   }
   pgh::record_kernel(LIMBS == 3 ? "k_mm_tc_bf16x6" : "k_mm_tc_bf16x3",
-                     (int64_t)grid.x * grid.y * grid.z, 128);
+                     (int64_t)grid.x * grid.y * grid.z, 320);
   int herr = 0;
   cudaMemcpyAsync(&herr, errp, sizeof(int), cudaMemcpyDeviceToHost, s);
   cudaFreeAsync(scratch, s);
