@@ -208,35 +208,8 @@ def run_ours(args, rank, world):
     op_ms = {op: statistics.mean(v) for op, v in per_op.items()}
     dominant = max(op_ms, key=op_ms.get)
 
-    # -------- e2e: host (pinned) -> device mirror -> 7 ops -> results to host
-    pinned_in = torch.empty(N0 * N1, dtype=torch.float64, pin_memory=True)
-    pinned_in.numpy()[:] = host.reshape(-1)
-    out_host = {op: torch.empty(outs[op].storage.nbytes // 1, dtype=torch.uint8, pin_memory=True)
-                for op in UFUNC_OPS}
-    mirror = copies[0].storage.dev
-    nbytes_in = N0 * N1 * 8
-    L = A.lib()
-
-    def e2e_step():
-        A.check(L.pdlgb300_to_device(mirror, pinned_in.data_ptr(), nbytes_in))
-        for op in UFUNC_OPS:
-            getattr(P, op)(copies[0], outs[op])
-        for op in UFUNC_OPS:
-            A.check(L.pdlgb300_to_host(out_host[op].data_ptr(), outs[op].storage.dev,
-                                       outs[op].storage.nbytes))
-
-    for _ in range(max(1, args.warmup)):
-        e2e_step()
-    torch.cuda.synchronize()
-    te = time.perf_counter()
-    for _ in range(args.steps):
-        e2e_step()
-    torch.cuda.synchronize()
-    e2e_ms = (time.perf_counter() - te) * 1e3 / args.steps
-    d2h = sum(outs[op].storage.nbytes for op in UFUNC_OPS)
-    e2e = {"value": world * step_bytes / (e2e_ms * 1e-3) / 1e9, "unit": "GB/s",
-           "h2d_bytes_per_step": nbytes_in, "d2h_bytes_per_step": d2h,
-           "ms_per_step": e2e_ms}
+    # -------- e2e: host (pinned) -> device mirror -> the ops -> results to host
+    e2e = run_e2e(args, P, A, torch, host, copies, outs, step_bytes, world) if args.e2e else None
 
     result = {
         "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world,
@@ -262,6 +235,38 @@ def run_ours(args, rank, world):
     if rank == 0 and not args.no_cpu:
         result["cpu_baseline"] = cpu_baseline(args, host)
     return result
+
+
+def run_e2e(args, P, A, torch, host, copies, outs, step_bytes, world):
+    """Through the C ABI from pinned host memory: copy the input to its
+    device mirror, run the ops, copy every result back; wall time per step."""
+    pinned_in = torch.empty(N0 * N1, dtype=torch.float64, pin_memory=True)
+    pinned_in.numpy()[:] = host.reshape(-1)
+    out_host = {op: torch.empty(outs[op].storage.nbytes, dtype=torch.uint8, pin_memory=True)
+                for op in UFUNC_OPS}
+    mirror = copies[0].storage.dev
+    nbytes_in = N0 * N1 * 8
+    L = A.lib()
+
+    def e2e_step():
+        A.check(L.pdlgb300_to_device(mirror, pinned_in.data_ptr(), nbytes_in))
+        for op in UFUNC_OPS:
+            getattr(P, op)(copies[0], outs[op])
+        for op in UFUNC_OPS:
+            A.check(L.pdlgb300_to_host(out_host[op].data_ptr(), outs[op].storage.dev,
+                                       outs[op].storage.nbytes))
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    torch.cuda.synchronize()
+    te = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_ms = (time.perf_counter() - te) * 1e3 / args.steps
+    d2h = sum(outs[op].storage.nbytes for op in UFUNC_OPS)
+    return {"value": world * step_bytes / (e2e_ms * 1e-3) / 1e9, "unit": "GB/s",
+            "h2d_bytes_per_step": nbytes_in, "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms}
 
 
 def bench_matmult(args, P, torch, stream, bf16, peak_kind):
@@ -360,6 +365,7 @@ def run_reference(args, rank, world):
 
 
 def main():
+    global UFUNC_OPS
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
@@ -370,7 +376,11 @@ def main():
     ap.add_argument("--mm-steps", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=8.0)
+    ap.add_argument("--ops", default=",".join(UFUNC_OPS),
+                    help="comma-separated subset of the Ufunc family (for profiling)")
+    ap.add_argument("--no-e2e", dest="e2e", action="store_false")
     args = ap.parse_args()
+    UFUNC_OPS = [o for o in args.ops.split(",") if o]
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
     if args.impl == "reference":
