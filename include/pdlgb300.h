@@ -203,6 +203,25 @@ pdlgb300_error pdlgb300_matmult_bwd(const pdlgb300_ndarray *gc, const pdlgb300_n
                                     const pdlgb300_ndarray *b, pdlgb300_ndarray *ga,
                                     pdlgb300_ndarray *gb);
 
+/* ---- sumover without allocation --------------------------------------- */
+/* No counterpart in the reference.  Same result as pdlgb300_run_sumover, for
+ * callers that cannot let the library allocate device memory (a host that
+ * hands the library a fixed device-memory budget, or code that must not
+ * trigger the device-wide synchronisation an allocation or free can
+ * cause).  Always runs the multi-block split form of the reduction, whose
+ * per-split partial sums live in one fixed 1 MiB device array (per device,
+ * held until the process exits); it calls no allocator.
+ * - a and b must be device-resident (ddata set); b must already have
+ *   sumover's output shape and type (no null output, no conversion).
+ * - Rows are limited by the scratch: a call needing more than 1 MiB of
+ *   partials (two per row at least) returns PDLGB300_EUSERERROR.
+ * - The first call on a device looks the array's device address up
+ *   (cudaGetSymbolAddress); make that first call before any stream capture.
+ * - Every call shares the array (it keeps the last call's partials; each
+ *   call overwrites every slot it reads), so calls that overlap on the GPU
+ *   (other streams, other host threads) race: serialise them. */
+pdlgb300_error pdlgb300_sumover_noalloc(const pdlgb300_ndarray *a, pdlgb300_ndarray *b);
+
 /* ---- options ------------------------------------------------------------ */
 /* float32 matmult arithmetic. */
 enum {

@@ -117,6 +117,7 @@ SIGNATURES = {
     "pdlgb300_device_count": (Error, [C.POINTER(C.c_int32)]),
     "pdlgb300_last_launch": (Error, [C.POINTER(LaunchInfo)]),
     "pdlgb300_set_timing": (Error, [C.c_int32]),
+    "pdlgb300_sumover_noalloc": (Error, [P, P]),
 }
 
 LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libpdlgb300.so"

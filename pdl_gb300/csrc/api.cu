@@ -1553,3 +1553,112 @@ pdlgb300_error pdlgb300_matmult_bwd(const pdlgb300_ndarray *gc, const pdlgb300_n
 }
 
 }  // extern "C"
+
+// ======================================================= no-allocation sumover
+// pdlgb300_sumover_noalloc: the multi-block split sumover (per-split partial
+// sums, then an in-order combine) with its partials in a fixed device array
+// instead of memory from the allocator.  For callers that cannot allocate
+// device memory: a process that hands the library a fixed device-memory
+// budget up front, or code that must not trigger the device-wide
+// synchronisation an allocation or free can cause.
+namespace {
+
+constexpr size_t NOALLOC_SCRATCH_BYTES = (size_t)1 << 20;  // 1 MiB, per device
+__device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
+
+std::mutex g_noalloc_mu;
+void *g_noalloc_addr[64] = {nullptr};
+
+// Host code cannot use g_noalloc_scratch's name as a device address: look the
+// address up once per device, with that device current.
+pdlgb300_error noalloc_scratch(void **out) {
+  int dev = 0;
+  cudaError_t ce = cudaGetDevice(&dev);
+  if (ce != cudaSuccess || dev < 0 || dev >= 64)
+    return err(PDLGB300_EFATAL, "sumover_noalloc: no current CUDA device");
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_addr[dev]) {
+    void *p = nullptr;
+    ce = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (ce != cudaSuccess || !p)
+      return err(PDLGB300_EFATAL, "sumover_noalloc: cudaGetSymbolAddress failed: %s",
+                 cudaGetErrorString(ce));
+    g_noalloc_addr[dev] = p;
+  }
+  *out = g_noalloc_addr[dev];
+  return ok();
+}
+
+}  // namespace
+
+extern "C" pdlgb300_error pdlgb300_sumover_noalloc(const pdlgb300_ndarray *a_in,
+                                                   pdlgb300_ndarray *b_in) {
+  if (!a_in || !b_in) return err(PDLGB300_EUSERERROR, "sumover_noalloc: NULL ndarray");
+  const pdlgb300_vtable *vt = &VT[O_SUMOVER];
+  if (!a_in->ddata || !b_in->ddata)
+    return err(PDLGB300_EUSERERROR,
+               "sumover_noalloc: a and b must both be device-resident (ddata set)");
+  if (b_in->state & PDLGB300_NOMYDIMS)
+    return err(PDLGB300_EUSERERROR, "sumover_noalloc: b must be shaped and allocated by the caller");
+  if (a_in->datatype < 0 || a_in->datatype > PDLGB300_D)
+    return err(PDLGB300_EUSERERROR, "sumover_noalloc: unsupported type %d", a_in->datatype);
+  if (b_in->datatype != intplus(a_in->datatype))
+    return err(PDLGB300_EUSERERROR, "sumover_noalloc: b must have type %s",
+               TNAMES[intplus(a_in->datatype)]);
+  pdlgb300_ndarray a = *a_in, b = *b_in;
+  pdlgb300_ndarray *pp[2] = {&a, &b};
+  Brc br;
+  RET_IF(plan_broadcast(vt, pp, br));
+  void *scratch = nullptr;
+  RET_IF(noalloc_scratch(&scratch));
+  RedArgs g;
+  memset(&g, 0, sizeof g);
+  const int which[2] = {0, 1};
+  g.L = collapse(br, 2, which);
+  g.rows = g.L.total;
+  g.n = br.ind_sizes[0];
+  g.inc_n = g.n <= 1 ? 1 : br.inc_sizes[0][0];
+  const size_t isz = TSIZES[a.datatype], osz = TSIZES[b.datatype];
+  g.a = (const char *)a.ddata + a.offs * (int64_t)isz;
+  g.b = (char *)b.ddata + b.offs * (int64_t)osz;
+  g.bad = !!(a.state & PDLGB300_BADVAL);
+  g.abad_bits = bad_bits(&a);
+  g.abad_isnan = bad_isnan(&a);
+  g.bbad_bits = bad_bits(&b);
+  g.bbad_isnan = bad_isnan(&b);
+  g.setbad = nullptr;  // sumover never reports PDLSTATESETBAD
+  g.f32_comp = (int)g_opt_comp;
+  if (g.rows == 0) return ok();
+  // always the split form: at least two partials per row, as many as the
+  // planner would use for long rows, within the fixed scratch
+  const size_t unit = red_acc_size(R_SUM, a.datatype, g.f32_comp) + sizeof(int64_t);
+  const int nsm = pgh::num_sms();
+  int64_t want = 2;
+  if (g.rows < 2 * (int64_t)nsm && g.n >= 65536)
+    want = std::max<int64_t>(2, std::min<int64_t>((4 * (int64_t)nsm + g.rows - 1) / g.rows,
+                                                  g.n / 8192));
+  const int64_t fit = (int64_t)((NOALLOC_SCRATCH_BYTES - 256) / (unit * (size_t)g.rows));
+  if (fit < 2)
+    return err(PDLGB300_EUSERERROR,
+               "sumover_noalloc: %lld rows need %zu bytes of scratch, above the %zu-byte limit "
+               "(at most %lld rows for this type)",
+               (long long)g.rows, (size_t)(2 * unit * g.rows), NOALLOC_SCRATCH_BYTES,
+               (long long)((NOALLOC_SCRATCH_BYTES - 256) / (2 * unit)));
+  g.nsplit = (int)std::min<int64_t>(want, fit);
+  const size_t accsz = unit - sizeof(int64_t);
+  g.partials = scratch;
+  size_t off = ((size_t)g.rows * g.nsplit * accsz + 15) & ~(size_t)15;
+  g.pcounts = (int64_t *)((char *)scratch + off);
+  g.group = g.n >= 16384 ? 256 : 128;
+  RedLaunch lc{0, (int)std::min<int64_t>(g.rows * g.nsplit, (int64_t)1 << 30), g.group};
+  memset(&tl_info, 0, sizeof tl_info);
+  snprintf(tl_info.op, sizeof tl_info.op, "sumover_noalloc");
+  tl_info.rows = g.rows;
+  tl_info.n = g.n;
+  tl_info.bytes = (double)g.rows * g.n * isz + (double)g.rows * osz;
+  pdlgb300_error e = launch_red_sum(R_SUM, a.datatype, g, lc, g_stream);
+  if (e.error) return e;
+  if (g.bad) b_in->state |= PDLGB300_BADVAL;
+  tl_last = tl_info;
+  return ok();
+}
