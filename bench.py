@@ -1,23 +1,28 @@
 """Benchmark of PDL's broadcast-loop hot path on GB300.
 
-Headline (one JSON line on rank 0): Ufunc reduction GB/s over dim 0 of the
-float64 (4096, 2048) ndarray, uniform[-1,1) from seed 1, no bad values: one
-step = sumover, prodover, average, minimum, maximum, minimum_ind and
-cumusumover, each reading its own one of 6 device copies of the input (384
-MiB in rotation, more than twice the 129 MB L2, so every op streams from
-HBM).  value = algorithmic bytes (inputs read once + outputs written once)
-/ device time (CUDA events on the library's stream).  e2e = the same ops
-through the C ABI starting from pinned host memory: the step copies the
-input to its device mirror, runs the seven ops and copies every result back.
+Headline (one JSON line on rank 0): Ufunc reduce GB/s on the float32
+accuracy-stress workload -- an ndarray of dims (65536, 4096) plus one row of
+2^27 elements, magnitudes lognormal(0, 4) with random signs, 1% BAD (badflag
+on), seeded: one step = sumover, average and cumusumover over dim 0 of both
+(compensated float32 accumulation, the default).  Inputs (1.5 GiB) exceed
+the 129 MB L2.  value = algorithmic bytes (inputs read once + outputs
+written once) / device time (CUDA events on the library's stream, a GPU
+sleep enqueued first so host launches run ahead).  e2e = the same ops
+through the C ABI from pinned host memory: copy the inputs to their device
+mirrors, run, copy every result back.
 
-The same line carries the float32 matmult measurement (a(t=1024,h=2048)
-batch 16 x b(w=2048,t=1024), N(0,1)): TFLOP/s of the split-bf16 tensor-core
-kernel and of the plain FP32 SIMT kernel, each with its max normwise error
-against an FP64 product on sampled rows.
+The same line carries: the accuracy of compensated vs plain float32 vs the
+float64 path on that workload; the float64 (4096, 2048) Ufunc family
+(sumover, prodover, average, minimum, maximum, minimum_ind, cumusumover on
+6 rotating device copies, 384 MiB > 2x L2); and the float32 matmult
+(a(t=1024,h=2048) batch 16 x b(w=2048,t=1024)): TFLOP/s of the split-bf16
+tensor-core kernels and of the plain FP32 SIMT kernel with their max
+normwise errors against FP64 on sampled rows.
 
 --impl reference times the reference's algorithm on the host cores (the C
-restatement of the reference loops, with the reference's auto-pthread
-split over all host threads) on the same workload and metric.
+restatement of the reference loops, with the reference's auto-pthread split
+over all host threads) on the same workload and metric, on a bounded
+sample of rows.
 """
 from __future__ import annotations
 
@@ -38,13 +43,17 @@ sys.path.insert(0, str(ROOT))
 
 UFUNC_OPS = ["sumover", "prodover", "average", "minimum", "maximum", "minimum_ind",
              "cumusumover"]
-N0, N1 = 4096, 2048            # PDL dims (n, rows)
+C5_OPS = ["sumover", "average", "cumusumover"]
+N0, N1 = 4096, 2048            # float64 family: PDL dims (n, rows)
 NCOPIES = 6
-METRIC = "Ufunc reduce GB/s over dim 0 (sumover, prodover, average, minimum, maximum, minimum_ind, cumusumover)"
-WORKLOAD = "PDL::Ufunc family over dim 0 of float64 ndarray dims (4096,2048), uniform[-1,1) seed 1, no bad values"
-# dram__bytes_read.sum + dram__bytes_write.sum of one sumover launch on this
-# workload, from the ncu capture summarised in profiles/ (None: not captured)
-NCU_TRAFFIC_SUMOVER = None
+C5_N, C5_ROWS, C5_LONG = 65536, 4096, 1 << 27
+METRIC = "Ufunc reduce GB/s over dim 0 (sumover, average, cumusumover; compensated float32, 1% BAD)"
+WORKLOAD = ("PDL::Ufunc sumover/average/cumusumover over dim 0 of float32 dims (65536,4096) "
+            "plus one row of 2^27, lognormal(0,4) magnitudes with random sign, 1% BAD, seed 7")
+FAMILY = "float64 dims (4096,2048) uniform[-1,1) seed 1, no bad values"
+# dram__bytes_read.sum + dram__bytes_write.sum per launch of the dominant
+# kernel on this workload, from the ncu captures summarised in profiles/
+NCU_TRAFFIC = {}
 
 
 def peaks():
@@ -60,11 +69,25 @@ def c1_input():
     return rng.uniform(-1.0, 1.0, size=(N1, N0))  # numpy order: PDL dims (4096, 2048)
 
 
-def op_bytes(op):
-    inb = N0 * N1 * 8
-    if op == "cumusumover":
-        return inb * 2
-    return inb + N1 * 8
+def c5_inputs():
+    """float32 (rows, n) matrix and one long row: lognormal(0, 4) magnitude,
+    random sign, 1% set to float's default badvalue (-FLT_MAX)."""
+    rng = np.random.default_rng(7)
+    bad = np.float32(-3.4028234663852886e38)
+
+    def gen(count):
+        v = np.exp(np.float32(4.0) * rng.standard_normal(count, dtype=np.float32))
+        v *= np.where(rng.random(count, dtype=np.float32) < 0.5, np.float32(-1), np.float32(1))
+        v[rng.random(count, dtype=np.float32) < 0.01] = bad
+        return v
+
+    return gen(C5_N * C5_ROWS).reshape(C5_ROWS, C5_N), gen(C5_LONG)
+
+
+def op_bytes(op, n=N0, rows=N1, isz=8, osz=8):
+    if op.startswith("cumu") or op.startswith("dcumu"):
+        return rows * n * (isz + osz)
+    return rows * n * isz + rows * (8 if op.endswith("_ind") else osz)
 
 
 class Clocks:
@@ -72,14 +95,11 @@ class Clocks:
 
     def __init__(self, gpu_index=0):
         self.proc = None
-        self.out = None
         self.idx = gpu_index
+        self.lines = []
 
     def __enter__(self):
         try:
-            self.out = open(ROOT / "gpurun_out" / "bench_clocks.csv", "w") if (ROOT / "gpurun_out").exists() \
-                else open(os.devnull, "w")
-            self.tmp = []
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.idx}",
                  "--query-gpu=clocks.sm,clocks.max.sm,clocks_event_reasons.active,"
@@ -87,9 +107,9 @@ class Clocks:
                  "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
                  "--format=csv,noheader,nounits", "-lms", "100"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
-            self.lines = []
             self.th = threading.Thread(target=self._read, daemon=True)
             self.th.start()
+            time.sleep(0.15)
         except Exception:
             self.proc = None
         return self
@@ -107,14 +127,15 @@ class Clocks:
             except Exception:
                 self.proc.kill()
             self.th.join(timeout=2)
-        if self.out:
-            self.out.write("\n".join(getattr(self, "lines", [])))
-            self.out.close()
+        out = ROOT / "gpurun_out"
+        if out.exists():
+            with open(out / "bench_clocks.csv", "a") as f:
+                f.write("\n".join(self.lines) + "\n")
 
     def summary(self):
         sm, mx, reasons = [], 0.0, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in getattr(self, "lines", []):
+        for line in self.lines:
             f = [x.strip() for x in line.split(",")]
             if len(f) < 7:
                 continue
@@ -130,7 +151,30 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-# ---------------------------------------------------------------- our arm
+def timed_steps(torch, stream, steps, warmup, one_step, nops):
+    """Run warmup untimed steps, then `steps` timed ones with a GPU sleep
+    enqueued first; returns total ms, per-op ms lists, launches, clocks."""
+    for k in range(warmup):
+        one_step(k, None)
+    torch.cuda.synchronize()
+    ev = [[(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(nops)] for _ in range(steps)]
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    launches = 0
+    with Clocks(torch.cuda.current_device()) as clk:
+        torch.cuda._sleep(int(2.0e9 * 0.05))
+        t0.record(stream)
+        for k in range(steps):
+            launches += one_step(k, ev[k])
+        t1.record(stream)
+        torch.cuda.synchronize()
+    total = t0.elapsed_time(t1)
+    per_op = [[ev[k][j][0].elapsed_time(ev[k][j][1]) for k in range(steps)] for j in range(nops)]
+    return total, per_op, launches, clk.summary()
+
+
+# ------------------------------------------------------------- our arm
 
 def run_ours(args, rank, world):
     import torch
@@ -143,23 +187,176 @@ def run_ours(args, rank, world):
     stream = torch.cuda.current_stream()
     P.set_stream(stream.cuda_stream)
     hbm, bf16, peak_kind = peaks()
+    L = A.lib()
 
+    # ---------------- headline: config 5, compensated float32 with BAD
+    mat, row = c5_inputs()
+    xs = []
+    for arr in (mat, row):
+        x = P.pdl(arr)
+        x.badflag(1)
+        x.to_device()
+        xs.append(x)
+    work = [(op, j) for op in C5_OPS for j in range(2)]
+    outs = {(op, j): getattr(P, op)(xs[j]) for op, j in work}
+    P.sync()
+    shapes = [(C5_N, C5_ROWS), (C5_LONG, 1)]
+    wbytes = [op_bytes(op, *shapes[j], isz=4, osz=4) for op, j in work]
+
+    def one_step(k, ev):
+        n = 0
+        for i, (op, j) in enumerate(work):
+            if ev is not None:
+                ev[i][0].record(stream)
+            getattr(P, op)(xs[j], outs[(op, j)])
+            if ev is not None:
+                ev[i][1].record(stream)
+            n += P.last_launch_info()["nlaunches"]
+        return n
+
+    if world > 1:
+        torch.distributed.barrier()
+    total, per_op, launches, clocks = timed_steps(torch, stream, args.steps, args.warmup,
+                                                  one_step, len(work))
+    if world > 1:
+        torch.distributed.barrier()
+        t = torch.tensor([total], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total = float(t.item())
+    step_bytes = sum(wbytes)
+    ms_per_step = total / args.steps
+    value = world * step_bytes / (ms_per_step * 1e-3) / 1e9
+    op_ms = {f"{op}[{'matrix' if j == 0 else 'row'}]": statistics.mean(per_op[i])
+             for i, (op, j) in enumerate(work)}
+    op_gbs = {k: wbytes[i] / (v * 1e-3) / 1e9 for i, (k, v) in enumerate(op_ms.items())}
+    dom = max(op_ms, key=op_ms.get)
+    result = {
+        "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded numpy lognormal(0,4), random sign, 1% BAD)",
+        "config": {"workload": WORKLOAD, "ops_per_step": [f"{op}[{'matrix' if j == 0 else 'row'}]"
+                                                          for op, j in work],
+                   "accumulation": "compensated float32 (default)",
+                   "l2": "inputs 1.5 GiB > 129 MB L2 (no reuse between ops)",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "per_op_gbs": op_gbs, "per_op_ms": op_ms,
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": op_gbs[dom], "peak": hbm,
+                     "unit": "GB/s", "frac": op_gbs[dom] / hbm, "peak_kind": peak_kind,
+                     "traffic": NCU_TRAFFIC.get(dom), "step_frac": value / world / hbm},
+        "gpu_launches": launches,
+        "clocks": clocks,
+    }
+    if args.e2e:
+        result["e2e"] = c5_e2e(args, P, A, torch, (mat, row), xs, outs, work, step_bytes, world)
+    if rank == 0 and args.accuracy:
+        result["accuracy"] = c5_accuracy(P, xs, (mat, row))
+    del xs, outs
+    torch.cuda.empty_cache()
+
+    if rank == 0 and args.family:
+        result["f64_family"] = run_family(args, P, torch, stream, hbm)
+    if args.matmult and rank == 0:
+        result["matmult"] = bench_matmult(args, P, torch, stream, bf16, peak_kind)
+    if rank == 0 and not args.no_cpu:
+        result["cpu_baseline"] = cpu_baseline(args, mat)
+    return result
+
+
+def c5_e2e(args, P, A, torch, arrays, xs, outs, work, step_bytes, world):
+    """Through the C ABI from pinned host memory: inputs to their device
+    mirrors, the ops, every result back to pinned host memory."""
+    L = A.lib()
+    pins = []
+    for arr in arrays:
+        t = torch.empty(arr.size, dtype=torch.float32, pin_memory=True)
+        t.numpy()[:] = arr.reshape(-1)
+        pins.append(t)
+    outh = {k: torch.empty(o.storage.nbytes, dtype=torch.uint8, pin_memory=True)
+            for k, o in outs.items()}
+
+    def e2e_step():
+        for j, x in enumerate(xs):
+            A.check(L.pdlgb300_to_device(x.storage.dev, pins[j].data_ptr(), x.storage.nbytes))
+        for op, j in work:
+            getattr(P, op)(xs[j], outs[(op, j)])
+        for k, o in outs.items():
+            A.check(L.pdlgb300_to_host(outh[k].data_ptr(), o.storage.dev, o.storage.nbytes))
+
+    e2e_step()
+    torch.cuda.synchronize()
+    n = max(2, args.steps // 4)
+    te = time.perf_counter()
+    for _ in range(n):
+        e2e_step()
+    torch.cuda.synchronize()
+    ms = (time.perf_counter() - te) * 1e3 / n
+    return {"value": world * step_bytes / (ms * 1e-3) / 1e9, "unit": "GB/s",
+            "h2d_bytes_per_step": sum(x.storage.nbytes for x in xs),
+            "d2h_bytes_per_step": sum(o.storage.nbytes for o in outs.values()),
+            "ms_per_step": ms, "steps": n}
+
+
+def c5_accuracy(P, xs, arrays):
+    """Max errors of compensated and plain float32 against the float64 path
+    (dsumover, daverage, dcumusumover on the GPU), per row: relative
+    |x - x64| / |x64| and normwise |x - x64| / sum|a|."""
+    mat, row = arrays
+    res = {}
+    bad = np.float32(-3.4028234663852886e38)
+    for op, dop in [("sumover", "dsumover"), ("average", "daverage")]:
+        for j, x in enumerate(xs):
+            ref = getattr(P, dop)(x).numpy().astype(np.float64)
+            a = (mat if j == 0 else row.reshape(1, -1))
+            scale = np.where(a == bad, 0, np.abs(a.astype(np.float64))).sum(-1)
+            if op == "average":
+                scale = scale / np.maximum((a != bad).sum(-1), 1)
+            key = f"{op}[{'matrix' if j == 0 else 'row'}]"
+            res[key] = {}
+            for mode, comp in [("compensated", True), ("plain", False)]:
+                P.set_compensated(comp)
+                got = getattr(P, op)(x).numpy().astype(np.float64)
+                P.set_compensated(True)
+                err = np.abs(got - ref)
+                res[key][mode] = {"max_rel_err": float(np.max(err / np.maximum(np.abs(ref), 1e-300))),
+                                  "max_normwise_err": float(np.max(err / scale))}
+    # running sums: 32 sampled rows of the matrix, and the long row
+    rs = np.random.default_rng(0).choice(C5_ROWS, 32, replace=False)
+    for j, x in enumerate(xs):
+        ref = P.dcumusumover(x).numpy()
+        ref = ref[rs] if j == 0 else ref.reshape(1, -1)
+        a = mat[rs] if j == 0 else row.reshape(1, -1)
+        good = a != bad
+        scale = np.cumsum(np.where(good, np.abs(a.astype(np.float64)), 0), -1)
+        key = f"cumusumover[{'matrix' if j == 0 else 'row'}]"
+        res[key] = {}
+        for mode, comp in [("compensated", True), ("plain", False)]:
+            P.set_compensated(comp)
+            got = P.cumusumover(x).numpy()
+            P.set_compensated(True)
+            got = got[rs] if j == 0 else got.reshape(1, -1)
+            err = np.abs(got.astype(np.float64) - ref)[good]
+            rel = err / np.maximum(np.abs(ref[good]), 1e-300)
+            res[key][mode] = {"max_rel_err": float(rel.max()),
+                              "max_normwise_err": float((err / np.maximum(scale[good], 1e-300)).max())}
+    res["reference_point"] = "float64 GPU path (d-variants), itself checked against the CPU oracle in tests"
+    return res
+
+
+def run_family(args, P, torch, stream, hbm):
+    """float64 (4096, 2048) Ufunc family on rotating device copies."""
     host = c1_input()
     copies = []
     for _ in range(NCOPIES):
-        x = P.pdl(host)
-        x.to_device()
-        x.storage.host = None  # device-resident only
+        x = P.pdl(host).to_device()
+        x.storage.host = None
         x.storage.fresh = "dev"
         copies.append(x)
-    outs = {}
-    for op in UFUNC_OPS:
-        r = getattr(P, op)(copies[0])
-        outs[op] = r  # device-resident preallocated outputs of the right shape/type
+    outs = {op: getattr(P, op)(copies[0]) for op in UFUNC_OPS}
     P.sync()
 
-    def step(k, times=None, ev=None):
-        launches = 0
+    def one_step(k, ev):
+        n = 0
         for j, op in enumerate(UFUNC_OPS):
             x = copies[(k * len(UFUNC_OPS) + j) % NCOPIES]
             if ev is not None:
@@ -167,106 +364,20 @@ def run_ours(args, rank, world):
             getattr(P, op)(x, outs[op])
             if ev is not None:
                 ev[j][1].record(stream)
-            launches += P.last_launch_info()["nlaunches"]
-        return launches
+            n += P.last_launch_info()["nlaunches"]
+        return n
 
-    for k in range(args.warmup):
-        step(k)
-    torch.cuda.synchronize()
-    # per-op device times (events around each op), then the whole K-step region
-    ev = [[(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-           for _ in UFUNC_OPS] for _ in range(args.steps)]
-    if world > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
-    t0 = torch.cuda.Event(enable_timing=True)
-    t1 = torch.cuda.Event(enable_timing=True)
-    launches = 0
-    with Clocks(dev.index) as clk:
-        # keep the GPU busy while the host enqueues the timed ops, so the
-        # events time back-to-back kernels, not host launch overhead
-        torch.cuda._sleep(int(2.0e9 * 0.06))
-        t0.record(stream)
-        for k in range(args.steps):
-            launches += step(k, ev=ev[k])
-        t1.record(stream)
-        torch.cuda.synchronize()
-    if world > 1:
-        torch.distributed.barrier()
-    total_ms = t0.elapsed_time(t1)
-    per_op = {op: [ev[k][j][0].elapsed_time(ev[k][j][1]) for k in range(args.steps)]
-              for j, op in enumerate(UFUNC_OPS)}
+    total, per_op, launches, clocks = timed_steps(torch, stream, args.steps, args.warmup,
+                                                  one_step, len(UFUNC_OPS))
     step_bytes = sum(op_bytes(op) for op in UFUNC_OPS)
-    kernel_ms = sum(sum(v) for v in per_op.values()) / args.steps
-    if world > 1:
-        t = torch.tensor([total_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
-    ms_per_step = total_ms / args.steps
-    value = world * step_bytes / (ms_per_step * 1e-3) / 1e9
-    op_gbs = {op: op_bytes(op) / (statistics.mean(v) * 1e-3) / 1e9 for op, v in per_op.items()}
-    op_ms = {op: statistics.mean(v) for op, v in per_op.items()}
-    dominant = max(op_ms, key=op_ms.get)
-
-    # -------- e2e: host (pinned) -> device mirror -> the ops -> results to host
-    e2e = run_e2e(args, P, A, torch, host, copies, outs, step_bytes, world) if args.e2e else None
-
-    result = {
-        "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64", "data": "synthetic (seeded numpy uniform[-1,1))",
-        "config": {"workload": WORKLOAD, "ops_per_step": UFUNC_OPS,
-                   "l2": f"inputs rotate over {NCOPIES} device copies "
-                         f"({NCOPIES * N0 * N1 * 8 >> 20} MiB > 2x L2)",
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
-        "per_op_gbs": op_gbs, "per_op_ms": op_ms, "kernel_ms_per_step": kernel_ms,
-        "roofline": {"bound": "hbm", "kernel": dominant,
-                     "achieved": op_gbs[dominant], "peak": hbm, "unit": "GB/s",
-                     "frac": op_gbs[dominant] / hbm, "peak_kind": peak_kind,
-                     "traffic": NCU_TRAFFIC_SUMOVER if dominant == "sumover" else None,
-                     "family_frac": value / world / hbm},
-        "e2e": e2e,
-        "gpu_launches": launches,
-        "clocks": clk.summary(),
-    }
-    if args.matmult and rank == 0:
-        result["matmult"] = bench_matmult(args, P, torch, stream, bf16, peak_kind)
-    if rank == 0 and not args.no_cpu:
-        result["cpu_baseline"] = cpu_baseline(args, host)
-    return result
-
-
-def run_e2e(args, P, A, torch, host, copies, outs, step_bytes, world):
-    """Through the C ABI from pinned host memory: copy the input to its
-    device mirror, run the ops, copy every result back; wall time per step."""
-    pinned_in = torch.empty(N0 * N1, dtype=torch.float64, pin_memory=True)
-    pinned_in.numpy()[:] = host.reshape(-1)
-    out_host = {op: torch.empty(outs[op].storage.nbytes, dtype=torch.uint8, pin_memory=True)
-                for op in UFUNC_OPS}
-    mirror = copies[0].storage.dev
-    nbytes_in = N0 * N1 * 8
-    L = A.lib()
-
-    def e2e_step():
-        A.check(L.pdlgb300_to_device(mirror, pinned_in.data_ptr(), nbytes_in))
-        for op in UFUNC_OPS:
-            getattr(P, op)(copies[0], outs[op])
-        for op in UFUNC_OPS:
-            A.check(L.pdlgb300_to_host(out_host[op].data_ptr(), outs[op].storage.dev,
-                                       outs[op].storage.nbytes))
-
-    for _ in range(max(1, args.warmup)):
-        e2e_step()
-    torch.cuda.synchronize()
-    te = time.perf_counter()
-    for _ in range(args.steps):
-        e2e_step()
-    torch.cuda.synchronize()
-    e2e_ms = (time.perf_counter() - te) * 1e3 / args.steps
-    d2h = sum(outs[op].storage.nbytes for op in UFUNC_OPS)
-    return {"value": world * step_bytes / (e2e_ms * 1e-3) / 1e9, "unit": "GB/s",
-            "h2d_bytes_per_step": nbytes_in, "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms}
+    ms = total / args.steps
+    op_ms = {op: statistics.mean(per_op[j]) for j, op in enumerate(UFUNC_OPS)}
+    return {"workload": FAMILY, "ops": UFUNC_OPS,
+            "l2": f"inputs rotate over {NCOPIES} device copies ({NCOPIES * N0 * N1 * 8 >> 20} MiB)",
+            "value": step_bytes / (ms * 1e-3) / 1e9, "unit": "GB/s", "ms_per_step": ms,
+            "frac_of_hbm": step_bytes / (ms * 1e-3) / 1e9 / hbm,
+            "per_op_gbs": {op: op_bytes(op) / (v * 1e-3) / 1e9 for op, v in op_ms.items()},
+            "per_op_ms": op_ms, "gpu_launches": launches, "clocks": clocks}
 
 
 def bench_matmult(args, P, torch, stream, bf16, peak_kind):
@@ -312,54 +423,54 @@ def bench_matmult(args, P, torch, stream, bf16, peak_kind):
 
 # ------------------------------------------------------------- CPU baseline
 
-def cpu_time_family(host, nthreads, budget_s):
-    """The oracle (the reference's loops in C with its pthread split) on the
-    full workload, repeated until budget_s; returns GB/s and steps."""
-    import pdl_gb300 as P  # host-only construction of descriptors
+def cpu_time(mat, nrows, nthreads, budget_s, steps=None):
+    """The oracle (the reference's loops in C, with its auto-pthread split)
+    on `nrows` rows of the config-5 matrix; GB/s over the C5 ops."""
+    import pdl_gb300 as P
     from oracle import oracle as O
-    x = P.pdl(host)
-    step_bytes = sum(op_bytes(op) for op in UFUNC_OPS)
-    steps, t0 = 0, time.perf_counter()
+    x = P.pdl(np.ascontiguousarray(mat[:nrows]))
+    x.badflag(1)
+    step_bytes = sum(op_bytes(op, C5_N, nrows, 4, 4) for op in C5_OPS)
+    done, t0 = 0, time.perf_counter()
     while True:
-        for op in UFUNC_OPS:
+        for op in C5_OPS:
             O.run(op, [x], nthreads=nthreads)
-        steps += 1
-        if time.perf_counter() - t0 > budget_s:
+        done += 1
+        el = time.perf_counter() - t0
+        if (steps is not None and done >= steps) or (steps is None and el > budget_s):
             break
-    el = time.perf_counter() - t0
-    return steps * step_bytes / el / 1e9, steps, el
+    return step_bytes * done / el / 1e9, done, el, step_bytes
 
 
-def cpu_baseline(args, host):
+def cpu_baseline(args, mat):
     n = os.cpu_count() or 1
-    gbs, steps, el = cpu_time_family(host, n, args.cpu_budget)
+    rows = 256
+    gbs, steps, el, _ = cpu_time(mat, rows, n, args.cpu_budget)
     return {"value": gbs, "unit": "GB/s", "cores": n, "kind": "port",
-            "sample": f"{steps} full steps of the 7-op family ({el:.1f} s), "
-                      f"auto-pthread split over {n} threads"}
+            "sample": f"{rows} of the 4096 rows of the (65536,4096) matrix, the 3 ops, "
+                      f"{steps} repetitions in {el:.1f} s, auto-pthread split over {n} threads"}
 
 
 def run_reference(args, rank, world):
-    host = c1_input()
+    mat, _ = c5_inputs()
     n = os.cpu_count() or 1
-    gbs0, _, _ = cpu_time_family(host, n, 0.0)  # warm
+    rows = 256
+    cpu_time(mat, rows, n, 0.0, steps=max(1, args.warmup))
     ts = []
-    step_bytes = sum(op_bytes(op) for op in UFUNC_OPS)
-    for _ in range(args.warmup):
-        cpu_time_family(host, n, 0.0)
     for _ in range(args.steps):
-        t0 = time.perf_counter()
-        cpu_time_family(host, n, 0.0)
-        ts.append(time.perf_counter() - t0)
-    ms = statistics.mean(ts) * 1e3
-    value = step_bytes / (ms * 1e-3) / 1e9
+        gbs, _, el, sb = cpu_time(mat, rows, n, 0.0, steps=1)
+        ts.append(el)
+    value = sb / statistics.mean(ts) / 1e9
     return {"impl": "reference", "metric": METRIC, "value": value, "unit": "GB/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded numpy uniform[-1,1))",
-            "config": {"workload": WORKLOAD, "ops_per_step": UFUNC_OPS},
+            "ms_per_step": statistics.mean(ts) * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded numpy lognormal(0,4), random sign, 1% BAD)",
+            "config": {"workload": WORKLOAD, "ops_per_step": C5_OPS,
+                       "sample": f"{rows} rows of the matrix per step"},
             "cpu_baseline": {"value": value, "unit": "GB/s", "cores": n, "kind": "port",
-                             "sample": "one full 7-op step per timed step, "
-                                       f"auto-pthread split over {n} threads"},
+                             "sample": f"{rows} of the 4096 rows of the (65536,4096) matrix "
+                                       f"per step, auto-pthread split over {n} threads"},
             "e2e": {"value": value, "unit": "GB/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
 
@@ -377,8 +488,10 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=8.0)
     ap.add_argument("--ops", default=",".join(UFUNC_OPS),
-                    help="comma-separated subset of the Ufunc family (for profiling)")
+                    help="comma-separated subset of the float64 family (for profiling)")
     ap.add_argument("--no-e2e", dest="e2e", action="store_false")
+    ap.add_argument("--no-accuracy", dest="accuracy", action="store_false")
+    ap.add_argument("--no-family", dest="family", action="store_false")
     args = ap.parse_args()
     UFUNC_OPS = [o for o in args.ops.split(",") if o]
     rank = int(os.environ.get("RANK", 0))

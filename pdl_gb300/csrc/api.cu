@@ -433,8 +433,27 @@ void span_of(const pdlgb300_ndarray *x, int64_t &lo, int64_t &hi) {
   }
 }
 
+// Keep freed stream-ordered memory cached in the device's default pool
+// (its default release threshold of 0 returns memory to the driver at every
+// synchronisation, which makes per-call temporaries expensive).
+std::mutex g_pool_mu;
+bool g_pool_set[64] = {false};
+void keep_pool_cached() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return;
+  std::lock_guard<std::mutex> lk(g_pool_mu);
+  if (g_pool_set[dev]) return;
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+    uint64_t thr = UINT64_MAX;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+  }
+  g_pool_set[dev] = true;
+}
+
 pdlgb300_error dalloc(size_t nbytes, void **p) {
   *p = nullptr;
+  keep_pool_cached();
   if (nbytes == 0) nbytes = 16;
   cudaError_t e = cudaMallocAsync(p, nbytes, g_stream);
   if (e != cudaSuccess) {
@@ -643,6 +662,7 @@ pdlgb300_error run_impl(const pdlgb300_vtable *vt, pdlgb300_ndarray *const *pdls
                         const int64_t *other) {
   const int op = op_of(vt);
   if (op < 0) return err(PDLGB300_EUSERERROR, "unknown vtable");
+  keep_pool_cached();
   memset(&tl_info, 0, sizeof tl_info);
   snprintf(tl_info.op, sizeof tl_info.op, "%s", vt->name);
   RunCtx c;
