@@ -69,9 +69,10 @@ def c1_input():
     return rng.uniform(-1.0, 1.0, size=(N1, N0))  # numpy order: PDL dims (4096, 2048)
 
 
-def c5_inputs():
+def c5_inputs(rows=None):
     """float32 (rows, n) matrix and one long row: lognormal(0, 4) magnitude,
     random sign, 1% set to float's default badvalue (-FLT_MAX)."""
+    rows = rows or C5_ROWS
     rng = np.random.default_rng(7)
     bad = np.float32(-3.4028234663852886e38)
 
@@ -81,7 +82,7 @@ def c5_inputs():
         v[rng.random(count, dtype=np.float32) < 0.01] = bad
         return v
 
-    return gen(C5_N * C5_ROWS).reshape(C5_ROWS, C5_N), gen(C5_LONG)
+    return gen(C5_N * rows).reshape(rows, C5_N), gen(C5_LONG)
 
 
 def op_bytes(op, n=N0, rows=N1, isz=8, osz=8):
@@ -190,17 +191,17 @@ def run_ours(args, rank, world):
     L = A.lib()
 
     # ---------------- headline: config 5, compensated float32 with BAD
-    mat, row = c5_inputs()
+    mat, row = c5_inputs(args.c5_rows)
     xs = []
     for arr in (mat, row):
         x = P.pdl(arr)
         x.badflag(1)
         x.to_device()
         xs.append(x)
-    work = [(op, j) for op in C5_OPS for j in range(2)]
+    work = [(op, j) for op in args.c5_ops.split(",") for j in range(2)]
     outs = {(op, j): getattr(P, op)(xs[j]) for op, j in work}
     P.sync()
-    shapes = [(C5_N, C5_ROWS), (C5_LONG, 1)]
+    shapes = [(C5_N, mat.shape[0]), (C5_LONG, 1)]
     wbytes = [op_bytes(op, *shapes[j], isz=4, osz=4) for op, j in work]
 
     def one_step(k, ev):
@@ -490,6 +491,9 @@ def main():
     ap.add_argument("--ops", default=",".join(UFUNC_OPS),
                     help="comma-separated subset of the float64 family (for profiling)")
     ap.add_argument("--no-e2e", dest="e2e", action="store_false")
+    ap.add_argument("--c5-rows", type=int, default=C5_ROWS,
+                    help="rows of the (65536, rows) matrix (smaller for profiling)")
+    ap.add_argument("--c5-ops", default=",".join(C5_OPS))
     ap.add_argument("--no-accuracy", dest="accuracy", action="store_false")
     ap.add_argument("--no-family", dest="family", action="store_false")
     args = ap.parse_args()

@@ -647,12 +647,21 @@ pdlgb300_error setbad_word(int **out) {
   std::lock_guard<std::mutex> lk(g_flag_mu);
   if (!g_flag_word[dev]) {
     cudaError_t e = cudaMalloc((void **)&g_flag_word[dev], 256);
+    if (e == cudaSuccess) e = cudaMemset(g_flag_word[dev], 0, 256);
     if (e != cudaSuccess) {
       g_flag_word[dev] = nullptr;
       return err(PDLGB300_EFATAL, "device allocation failed: %s", cudaGetErrorString(e));
     }
   }
   *out = g_flag_word[dev];
+  return ok();
+}
+
+// Word 1 of the same allocation: set by kernels whose bounded waits gave up.
+pdlgb300_error status_word(int **out) {
+  int *w = nullptr;
+  RET_IF(setbad_word(&w));
+  *out = w + 1;
   return ok();
 }
 
@@ -924,11 +933,15 @@ pdlgb300_error dispatch_cumusum(RunCtx &c, int dop) {
     g.mode = -1;
     return launch_cumusum(dop, c.v[0].datatype, g, g_stream);
   }
+  RET_IF(status_word(&g.err));
   void *scratch = nullptr;
-  if (g.rows < 2 * (int64_t)nsm && g.n >= 65536) {
-    int64_t want = (4 * (int64_t)nsm + g.rows - 1) / g.rows;
-    int64_t nch = std::max<int64_t>(1, std::min<int64_t>(want, g.n / 16384));
+  // few rows: cut them into chunks so that ~24 warps per SM have work
+  const int64_t target = 24LL * nsm;
+  if (g.rows < target && g.n >= 32768) {
+    int64_t nch = std::max<int64_t>(1, std::min<int64_t>((target + g.rows - 1) / g.rows,
+                                                          g.n / 8192));
     g.chunk = (g.n + nch - 1) / nch;
+    g.chunk = (g.chunk + 4095) / 4096 * 4096;  // chunk starts stay 16-byte aligned
     g.nchunk = (int)((g.n + g.chunk - 1) / g.chunk);
     if (g.nchunk > 1) {
       size_t accsz = scan_acc_size(dop, c.v[0].datatype, g.f32_comp);
@@ -1383,6 +1396,14 @@ pdlgb300_error pdlgb300_to_host(void *host, const void *dptr, size_t nbytes) {
 pdlgb300_error pdlgb300_sync(void) {
   cudaError_t e = cudaStreamSynchronize(g_stream);
   if (e != cudaSuccess) return err(PDLGB300_EFATAL, "sync: %s", cudaGetErrorString(e));
+  int *w = nullptr;
+  if (!setbad_word(&w).error) {
+    int st = 0;
+    if (cudaMemcpy(&st, w + 1, sizeof(int), cudaMemcpyDeviceToHost) == cudaSuccess && st) {
+      cudaMemset(w + 1, 0, sizeof(int));
+      return err(PDLGB300_EFATAL, "a kernel gave up waiting on its pipeline (timeout)");
+    }
+  }
   return ok();
 }
 pdlgb300_error pdlgb300_device_count(int32_t *n) {

@@ -83,6 +83,8 @@ struct ScanArgs {
   int64_t chunk;     // elements per chunk
   void *partials;    // per (row, chunk) totals, then exclusive carries
   int mode;          // 0 full row, 1 chunk totals only, 2 chunk scan with carry
+  int bulk;          // rows are 16-byte aligned: TMA bulk-copy pipeline
+  int *err;          // device status word: set when a bounded wait gives up
 };
 pdlgb300_error launch_cumusum(int dop, int in_dt, ScanArgs g, cudaStream_t s);
 size_t scan_acc_size(int dop, int in_dt, int f32_comp);

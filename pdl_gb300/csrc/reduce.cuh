@@ -373,7 +373,7 @@ __device__ __forceinline__ void row_accumulate(const In *row, int64_t lo, int64_
                                                int lane, int G, const Bad<In> &bv,
                                                AccCnt<typename Op::Acc> &ac) {
   constexpr int VEC = 16 / sizeof(In);
-  constexpr int U = Op::kU ? Op::kU : (sizeof(In) >= 8 ? 4 : 2);  // vectors in flight
+  constexpr int U = Op::kU ? Op::kU : 8;  // 16-byte vectors in flight per thread
   int64_t i = lo;
   // scalar head up to a 16-byte boundary
   int64_t mis = ((uintptr_t)(row + lo) & 15) / sizeof(In);

@@ -2,15 +2,9 @@
 // b(n) = inclusive running sum of a(n); a bad element gives a bad output
 // and leaves the running sum unchanged.
 //
-// Contiguous rows: one block walks a row in tiles of 256 x 8 elements,
-// staged through shared memory for coalesced loads and stores.  Each thread
-// first totals its 8 elements (float64: one F64Sum block, integer pipe), the
-// block scans the thread totals, then each thread re-walks its elements
-// from its exclusive prefix with one add per element.  Long rows with few
-// rows are cut into chunks: chunk totals, a per-row exclusive scan of the
-// totals, then every chunk scanned from its carry (three passes, no
-// inter-block waiting).  Strided rows: one thread per row in the
-// reference's order.
+// Contiguous rows run warp-synchronously, one warp per row (k_scan_warp);
+// long rows with few rows are cut into chunks whose totals are summed
+// first.  Strided rows: one thread per row in the reference's order.
 #include "args.cuh"
 #include "f64sum.cuh"
 
@@ -71,23 +65,50 @@ template <class T> __device__ __forceinline__ T shfl_up_any(T v, int d) {
   return u.t;
 }
 
+template <class T> __device__ __forceinline__ T shfl_any(T v, int src) {
+  constexpr int W = (sizeof(T) + 3) / 4;
+  union { T t; uint32_t w[W]; } u;
+  u.t = v;
+#pragma unroll
+  for (int i = 0; i < W; i++) u.w[i] = __shfl_sync(0xffffffffu, u.w[i], src);
+  return u.t;
+}
+template <class T> __device__ __forceinline__ T shfl_down_any2(T v, int d) {
+  constexpr int W = (sizeof(T) + 3) / 4;
+  union { T t; uint32_t w[W]; } u;
+  u.t = v;
+#pragma unroll
+  for (int i = 0; i < W; i++) u.w[i] = __shfl_down_sync(0xffffffffu, u.w[i], d);
+  return u.t;
+}
+
 constexpr int SB = 256, SI = 8, STILE = SB * SI;
 
+// Contiguous rows: one warp per row (or per chunk of a long row), warp-
+// synchronous only -- no shared memory, no block barriers.  Each step a lane
+// takes 32 contiguous bytes (two 16-byte vectors; 16 bytes for 1-2 byte
+// types), totals them, the warp scans the lane totals with shuffles, and
+// each lane writes its running sums with 16-byte stores; the next step's
+// vectors are loaded before the current step is scanned.  The carry stays
+// in registers.  Long rows with few rows are cut into chunks: chunk totals
+// first (mode 1), then each chunk scanned from the sum of its row's earlier
+// chunk totals, which its warp adds up itself (mode 2).
 template <class In, class Out, bool BAD, bool COMP>
-__global__ void __launch_bounds__(SB) k_scan_rows(const ScanArgs g) {
+__global__ void __launch_bounds__(256) k_scan_warp(const ScanArgs g) {
   using S = ScanT<In, Out, COMP>;
   using Acc = typename S::Acc;
-  __shared__ In s_in[STILE];
-  __shared__ Out s_out[STILE];
-  __shared__ Acc s_warp[SB / 32];
-  __shared__ Acc s_carry;
+  constexpr int VEC = 16 / sizeof(In);
+  constexpr int PER = sizeof(In) >= 4 ? 2 * VEC : VEC;  // elements per lane per step
+  constexpr int STEP = 32 * PER;
   Bad<In> bv{from_bits<In>(g.abad), (bool)g.abad_isnan};
   const Out obad = from_bits<Out>(g.bbad);
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int lane = threadIdx.x & 31;
+  const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
   const int64_t units = g.rows * g.nchunk;
-  for (int64_t u = blockIdx.x; u < units; u += gridDim.x) {
-    int64_t row = u / g.nchunk;
-    int chunk = (int)(u - row * g.nchunk);
+  for (int64_t u = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); u < units;
+       u += nwarps) {
+    const int64_t row = u / g.nchunk;
+    const int chunk = (int)(u - row * g.nchunk);
     int64_t offs[MAXP];
     loop_offsets(g.L, row, offs);
     const In *a = reinterpret_cast<const In *>(g.a) + offs[0];
@@ -95,102 +116,96 @@ __global__ void __launch_bounds__(SB) k_scan_rows(const ScanArgs g) {
     int64_t lo = (int64_t)chunk * g.chunk;
     int64_t hi = lo + g.chunk < g.n ? lo + g.chunk : g.n;
     if (g.nchunk == 1) { lo = 0; hi = g.n; }
+    const bool va = ((uintptr_t)(a + lo) % 16) == 0;
+    const bool vb = ((uintptr_t)(b + lo) % 16) == 0 && ((PER * sizeof(Out)) % 16) == 0;
     Acc carry = S::zero();
-    if (g.mode == 2) carry = reinterpret_cast<const Acc *>(g.partials)[u];
-    for (int64_t t0 = lo; t0 < hi; t0 += STILE) {
-      const int64_t cnt = hi - t0 < STILE ? hi - t0 : STILE;
-      __syncthreads();
+    if (g.mode == 2 && chunk > 0) {
+      const Acc *p = reinterpret_cast<const Acc *>(g.partials) + row * g.nchunk;
+      Acc sacc = S::zero();
+      for (int c = lane; c < chunk; c += 32) sacc = S::add(sacc, p[c]);
 #pragma unroll
-      for (int k = 0; k < SI; k++) {
-        int j = tid + k * SB;
-        if (j < cnt) s_in[j] = __ldcs(a + t0 + j);
-      }
-      __syncthreads();
-      In v[SI];
-      bool ok[SI];
+      for (int d = 16; d > 0; d >>= 1) sacc = S::add(sacc, shfl_down_any2(sacc, d));
+      carry = shfl_any(sacc, 0);
+    }
+    auto load = [&](In (&v)[PER], int64_t s0) {
+      const int64_t base = s0 + (int64_t)lane * PER;
+      if (va && base + PER <= hi) {
 #pragma unroll
-      for (int j = 0; j < SI; j++) {
-        int idx = tid * SI + j;
-        v[j] = idx < cnt ? s_in[idx] : (In)0;
-        ok[j] = idx < cnt && !(BAD && bv.is(v[j]));
+        for (int q = 0; q < PER * (int)sizeof(In) / 16; q++) {
+          float4 f = __ldcs(reinterpret_cast<const float4 *>(a + base) + q);
+          memcpy(reinterpret_cast<char *>(v) + 16 * q, &f, 16);
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < PER; j++) v[j] = base + j < hi ? a[base + j] : (In)0;
       }
-      // thread total
+    };
+    In cur[PER], nxt[PER];
+    if (lo < hi) load(cur, lo);
+    Acc lanesum = S::zero();  // mode 1: totals only
+    for (int64_t s0 = lo; s0 < hi; s0 += STEP) {
+      if (s0 + STEP < hi) load(nxt, s0 + STEP);
+      const int64_t base = s0 + (int64_t)lane * PER;
+      bool good[PER];
+#pragma unroll
+      for (int j = 0; j < PER; j++) good[j] = base + j < hi && !(BAD && bv.is(cur[j]));
       Acc tot = S::zero();
       if constexpr (std::is_same_v<Out, double> && std::is_same_v<In, double> && !BAD) {
         F64Sum fs{0.0};
-        double w[SI];
+        double w[PER];
 #pragma unroll
-        for (int j = 0; j < SI; j++) w[j] = ok[j] ? v[j] : 0.0;
-        fs.add_block<SI>(w);
+        for (int j = 0; j < PER; j++) w[j] = good[j] ? cur[j] : 0.0;
+        fs.add_block<PER>(w);
         tot = fs.s;
       } else {
 #pragma unroll
-        for (int j = 0; j < SI; j++)
-          if (ok[j]) tot = S::add1(tot, v[j]);
+        for (int j = 0; j < PER; j++)
+          if (good[j]) tot = S::add1(tot, cur[j]);
       }
-      // block exclusive scan of thread totals
-      Acc inc = tot;
+      if (g.mode == 1) {
+        lanesum = S::add(lanesum, tot);
+      } else {
+        Acc inc = tot;
 #pragma unroll
-      for (int d = 1; d < 32; d <<= 1) {
-        Acc o = shfl_up_any(inc, d);
-        if (lane >= d) inc = S::add(o, inc);
-      }
-      if (lane == 31) s_warp[warp] = inc;
-      __syncthreads();
-      if (warp == 0) {
-        Acc w = lane < SB / 32 ? s_warp[lane] : S::zero();
-#pragma unroll
-        for (int d = 1; d < SB / 32; d <<= 1) {
-          Acc o = shfl_up_any(w, d);
-          if (lane >= d) w = S::add(o, w);
+        for (int d = 1; d < 32; d <<= 1) {
+          Acc o = shfl_up_any(inc, d);
+          if (lane >= d) inc = S::add(o, inc);
         }
-        if (lane < SB / 32) s_warp[lane] = w;  // inclusive warp prefixes
-      }
-      __syncthreads();
-      Acc excl = shfl_up_any(inc, 1);
-      if (lane == 0) excl = S::zero();
-      if (warp > 0) excl = S::add(s_warp[warp - 1], excl);
-      Acc blocktot = s_warp[SB / 32 - 1];
-      if (g.mode != 1) {
+        Acc excl = shfl_up_any(inc, 1);
+        if (lane == 0) excl = S::zero();
+        const Acc wtot = shfl_any(inc, 31);
         Acc run = S::add(carry, excl);
+        Out o[PER];
 #pragma unroll
-        for (int j = 0; j < SI; j++) {
-          int idx = tid * SI + j;
-          if (idx < cnt) {
-            if (ok[j]) {
-              run = S::add1(run, v[j]);
-              s_out[idx] = S::value(run);
-            } else {
-              s_out[idx] = obad;
-            }
+        for (int j = 0; j < PER; j++) {
+          if (good[j]) {
+            run = S::add1(run, cur[j]);
+            o[j] = S::value(run);
+          } else {
+            o[j] = obad;
           }
         }
-        __syncthreads();
+        if (vb && base + PER <= hi) {
 #pragma unroll
-        for (int k = 0; k < SI; k++) {
-          int j = tid + k * SB;
-          if (j < cnt) b[t0 + j] = s_out[j];
+          for (int q = 0; q < PER * (int)sizeof(Out) / 16; q++) {
+            float4 f;
+            memcpy(&f, reinterpret_cast<const char *>(o) + 16 * q, 16);
+            __stcs(reinterpret_cast<float4 *>(b + base) + q, f);
+          }
+        } else {
+#pragma unroll
+          for (int j = 0; j < PER; j++)
+            if (base + j < hi) b[base + j] = o[j];
         }
+        carry = S::add(carry, wtot);
       }
-      carry = S::add(carry, blocktot);
+#pragma unroll
+      for (int j = 0; j < PER; j++) cur[j] = nxt[j];
     }
-    if (g.mode == 1 && tid == 0) reinterpret_cast<Acc *>(g.partials)[u] = carry;
-  }
-}
-
-// Per-row exclusive scan of chunk totals, in place.
-template <class In, class Out, bool COMP>
-__global__ void k_scan_carries(const ScanArgs g) {
-  using S = ScanT<In, Out, COMP>;
-  using Acc = typename S::Acc;
-  for (int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; row < g.rows;
-       row += (int64_t)gridDim.x * blockDim.x) {
-    Acc *p = reinterpret_cast<Acc *>(g.partials) + row * g.nchunk;
-    Acc run = S::zero();
-    for (int c = 0; c < g.nchunk; c++) {
-      Acc t = p[c];
-      p[c] = run;
-      run = S::add(run, t);
+    if (g.mode == 1) {
+#pragma unroll
+      for (int d = 16; d > 0; d >>= 1) lanesum = S::add(lanesum, shfl_down_any2(lanesum, d));
+      if (lane == 0) reinterpret_cast<Acc *>(g.partials)[u] = lanesum;
     }
   }
 }
@@ -233,29 +248,26 @@ pdlgb300_error scan_typed(ScanArgs g, cudaStream_t s) {
     pgh::record_kernel("k_scan_thread", grid, 128);
     return e;
   }
-  auto rows_kernel = [&](ScanArgs a) {
-    int64_t units = a.rows * a.nchunk;
-    int64_t grid = std::min<int64_t>(units, (int64_t)nsm * 64);
-    if (a.bad) k_scan_rows<In, Out, true, COMP><<<(int)grid, SB, 0, s>>>(a);
-    else k_scan_rows<In, Out, false, COMP><<<(int)grid, SB, 0, s>>>(a);
-    pgh::record_kernel("k_scan_rows", grid, SB);
+  // contiguous rows: warp per row (per chunk for long rows)
+  auto warp_kernel = [&](ScanArgs a) {
+    const int64_t units = a.rows * a.nchunk;
+    const int64_t grid = std::min<int64_t>((units + 7) / 8, (int64_t)nsm * 16);
+    if (a.bad) k_scan_warp<In, Out, true, COMP><<<(int)grid, SB, 0, s>>>(a);
+    else k_scan_warp<In, Out, false, COMP><<<(int)grid, SB, 0, s>>>(a);
+    pgh::record_kernel("k_scan_warp", grid, SB);
     return cudaGetLastError();
   };
   if (g.nchunk <= 1) {
     g.mode = 0;
     g.nchunk = 1;
-    if (!pgh::cuda_check(rows_kernel(g), &e, "k_scan_rows")) return e;
+    if (!pgh::cuda_check(warp_kernel(g), &e, "k_scan_warp")) return e;
     return e;
   }
   ScanArgs a = g;
   a.mode = 1;
-  if (!pgh::cuda_check(rows_kernel(a), &e, "k_scan_rows(totals)")) return e;
-  int64_t grid = std::min<int64_t>((g.rows + 127) / 128, 4096);
-  k_scan_carries<In, Out, COMP><<<(int)grid, 128, 0, s>>>(g);
-  if (!pgh::cuda_check(cudaGetLastError(), &e, "k_scan_carries")) return e;
-  pgh::record_kernel("k_scan_carries", grid, 128);
+  if (!pgh::cuda_check(warp_kernel(a), &e, "k_scan_warp(totals)")) return e;
   a.mode = 2;
-  if (!pgh::cuda_check(rows_kernel(a), &e, "k_scan_rows(carry)")) return e;
+  if (!pgh::cuda_check(warp_kernel(a), &e, "k_scan_warp(scan)")) return e;
   return e;
 }
 
