@@ -871,9 +871,16 @@ pdlgb300_error dispatch_reduce(RunCtx &c, int redop) {
     a.group = a.n >= 16384 ? 256 : 128;
     lc.block = a.group;
     int64_t units = a.rows;
-    // few long rows: split each row over several blocks
+    // few long rows: split each row over several blocks, as many splits as
+    // fill whole waves of resident blocks
     if (a.rows < 2 * (int64_t)nsm && a.n >= 65536) {
-      int64_t want = (4 * (int64_t)nsm + a.rows - 1) / a.rows;
+      const int dt0 = c.v[0].datatype;
+      int occ = (redop == R_SUM || redop == R_DSUM || redop == R_AVG || redop == R_DAVG)
+                    ? red_occ_sum(redop, dt0, a.f32_comp, a.bad, lc.block)
+                : (redop == R_PROD || redop == R_DPROD) ? red_occ_prod(redop, dt0, a.bad, lc.block)
+                                                        : red_occ_minmax(redop, dt0, a.bad, lc.block);
+      const int64_t slots = (int64_t)nsm * occ;
+      int64_t want = std::max<int64_t>(1, slots / a.rows);
       int64_t maxs = a.n / 8192;
       a.nsplit = (int)std::max<int64_t>(1, std::min(want, maxs));
       units = a.rows * a.nsplit;

@@ -46,6 +46,9 @@ pdlgb300_error launch_red_prod(int op, int in_dt, RedArgs args, const RedLaunch 
 pdlgb300_error launch_red_minmax(int op, int in_dt, RedArgs args, const RedLaunch &lc,
                                  cudaStream_t s);
 size_t red_acc_size(int op, int in_dt, int f32_comp);
+int red_occ_sum(int op, int in_dt, int comp, bool bad, int block);
+int red_occ_prod(int op, int in_dt, bool bad, int block);
+int red_occ_minmax(int op, int in_dt, bool bad, int block);
 
 // ------------------------------------------------------------ plus/mult
 struct BiopArgs {

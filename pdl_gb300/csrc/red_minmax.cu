@@ -21,6 +21,20 @@ pdlgb300_error launch_red_minmax(int op, int in_dt, RedArgs args, const RedLaunc
   return pgh::err(PDLGB300_EUSERERROR, "reduction: unsupported type %d", in_dt);
 }
 
+int red_occ_minmax(int op, int in_dt, bool bad, int block) {
+  int r = 1;
+  PG_DISPATCH(in_dt, {
+    using T = typename TT<DT>::T;
+    switch (op) {
+      case R_MIN: r = red_occ_typed<OpMM<T, false, false>, T, T>(bad, block); break;
+      case R_MAX: r = red_occ_typed<OpMM<T, true, false>, T, T>(bad, block); break;
+      case R_MIN_IND: r = red_occ_typed<OpMM<T, false, true>, T, int64_t>(bad, block); break;
+      case R_MAX_IND: r = red_occ_typed<OpMM<T, true, true>, T, int64_t>(bad, block); break;
+    }
+  });
+  return r;
+}
+
 // Size of one split-mode partial accumulator.
 size_t red_acc_size(int op, int in_dt, int comp) {
   size_t r = 0;

@@ -17,4 +17,15 @@ pdlgb300_error launch_red_prod(int op, int in_dt, RedArgs args, const RedLaunch 
   return pgh::err(PDLGB300_EUSERERROR, "reduction: unsupported type %d", in_dt);
 }
 
+int red_occ_prod(int op, int in_dt, bool bad, int block) {
+  int r = 1;
+  PG_DISPATCH(in_dt, {
+    using In = typename TT<DT>::T;
+    using OutP = typename TT<intplus(DT)>::T;
+    if (op == R_PROD) r = red_occ_typed<OpProd<In, OutP>, In, OutP>(bad, block);
+    else r = red_occ_typed<OpProd<In, double>, In, double>(bad, block);
+  });
+  return r;
+}
+
 }  // namespace pg

@@ -31,4 +31,28 @@ pdlgb300_error launch_red_sum(int op, int in_dt, RedArgs args, const RedLaunch &
   return pgh::err(PDLGB300_EUSERERROR, "reduction: unsupported type %d", in_dt);
 }
 
+int red_occ_sum(int op, int in_dt, int comp, bool bad, int block) {
+  int r = 1;
+  PG_DISPATCH(in_dt, {
+    using In = typename TT<DT>::T;
+    using OutP = typename TT<intplus(DT)>::T;
+    constexpr bool F32 = std::is_same_v<OutP, float>;
+    switch (op) {
+      case R_SUM:
+        if constexpr (F32)
+          if (comp) { r = red_occ_typed<OpSum<In, OutP, true>, In, OutP>(bad, block); break; }
+        r = red_occ_typed<OpSum<In, OutP, false>, In, OutP>(bad, block);
+        break;
+      case R_DSUM: r = red_occ_typed<OpSum<In, double, false>, In, double>(bad, block); break;
+      case R_AVG:
+        if constexpr (F32)
+          if (comp) { r = red_occ_typed<OpAvg<In, OutP, true>, In, OutP>(bad, block); break; }
+        r = red_occ_typed<OpAvg<In, OutP, false>, In, OutP>(bad, block);
+        break;
+      case R_DAVG: r = red_occ_typed<OpAvg<In, double, false>, In, double>(bad, block); break;
+    }
+  });
+  return r;
+}
+
 }  // namespace pg

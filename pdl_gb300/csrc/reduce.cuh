@@ -579,4 +579,13 @@ pdlgb300_error launch_red_typed(RedArgs args, const RedLaunch &lc, cudaStream_t 
 
 template <class Op> size_t acc_size() { return sizeof(typename Op::Acc); }
 
+// Resident blocks per SM of the row kernel for this op (for sizing splits).
+template <class Op, class In, class Out>
+int red_occ_typed(bool bad, int block) {
+  int occ = 0;
+  if (bad) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_red_rows<Op, In, Out, true>, block, 0);
+  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_red_rows<Op, In, Out, false>, block, 0);
+  return occ > 0 ? occ : 1;
+}
+
 }  // namespace pg
