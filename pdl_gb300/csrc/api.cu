@@ -912,6 +912,58 @@ pdlgb300_error dispatch_reduce(RunCtx &c, int redop) {
   return e;
 }
 
+// Rows start on 16-byte boundaries in both ndarrays (base and every
+// broadcast increment).
+bool chain_aligned(const Loop &L, const void *a, const void *b, size_t asz, size_t bsz) {
+  if ((uintptr_t)a % 16 || (uintptr_t)b % 16) return false;
+  for (int d = 0; d < L.nd; d++) {
+    if (L.size[d] <= 1) continue;
+    if ((L.inc[0][d] * (int64_t)asz) % 16 || (L.inc[1][d] * (int64_t)bsz) % 16) return false;
+  }
+  return true;
+}
+
+// Look-back slots of the chained scan, per device: a power-of-two ring at
+// least as large as one launch's chunk count, tagged by a 64-bit unit id
+// that only grows, so slots never need clearing between launches.
+struct ChainRing {
+  ChainSlot *slots = nullptr;
+  uint64_t cap = 0;
+  uint64_t next = 1;  // unit id 0 never used: zeroed memory reads as empty
+};
+ChainRing g_chain[64];
+std::mutex g_chain_mu;
+
+pdlgb300_error chain_slots(uint64_t units, ScanArgs *g) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64)
+    return err(PDLGB300_EFATAL, "no current CUDA device");
+  std::lock_guard<std::mutex> lk(g_chain_mu);
+  ChainRing &r = g_chain[dev];
+  if (r.cap < units) {
+    uint64_t cap = 1024;
+    while (cap < units) cap <<= 1;
+    if (r.slots) {
+      cudaStreamSynchronize(g_stream);
+      cudaFree(r.slots);
+      r.slots = nullptr;
+      r.cap = 0;
+    }
+    cudaError_t e = cudaMalloc((void **)&r.slots, cap * sizeof(ChainSlot));
+    if (e == cudaSuccess) e = cudaMemset(r.slots, 0, cap * sizeof(ChainSlot));
+    if (e != cudaSuccess) {
+      r.slots = nullptr;
+      return err(PDLGB300_EFATAL, "device allocation failed: %s", cudaGetErrorString(e));
+    }
+    r.cap = cap;
+  }
+  g->status = r.slots;
+  g->status_mask = r.cap - 1;
+  g->gid_base = r.next;
+  r.next += units;
+  return ok();
+}
+
 pdlgb300_error dispatch_cumusum(RunCtx &c, int dop) {
   const Brc &b = c.b;
   ScanArgs g;
@@ -941,6 +993,18 @@ pdlgb300_error dispatch_cumusum(RunCtx &c, int dop) {
     return launch_cumusum(dop, c.v[0].datatype, g, g_stream);
   }
   RET_IF(status_word(&g.err));
+  // 16-byte aligned rows of 4- and 8-byte types, not too short: the chained
+  // single-pass scan (one block per chunk, look-back across a row's chunks)
+  const int64_t cch = scan_chain_chunk(dop, c.v[0].datatype, g.f32_comp);
+  if (cch > 0 && g.n >= cch / 4 && chain_aligned(g.L, c.dev[0], c.dev[1],
+                                                  TSIZES[c.v[0].datatype],
+                                                  TSIZES[c.v[1].datatype])) {
+    g.mode = 3;
+    g.chunk = cch;
+    g.nchunk = (int)((g.n + cch - 1) / cch);
+    if (g.nchunk > 1) RET_IF(chain_slots((uint64_t)g.rows * g.nchunk, &g));
+    return launch_cumusum(dop, c.v[0].datatype, g, g_stream);
+  }
   void *scratch = nullptr;
   // few rows: cut them into chunks so that ~24 warps per SM have work
   const int64_t target = 24LL * nsm;

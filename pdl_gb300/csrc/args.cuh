@@ -85,10 +85,19 @@ struct ScanArgs {
   int nchunk;        // chunks per row (> 1: three-pass long-row scan)
   int64_t chunk;     // elements per chunk
   void *partials;    // per (row, chunk) totals, then exclusive carries
-  int mode;          // 0 full row, 1 chunk totals only, 2 chunk scan with carry
-  int bulk;          // rows are 16-byte aligned: TMA bulk-copy pipeline
+  int mode;          // 0 full row, 1 chunk totals only, 2 chunk scan with carry, 3 chained
   int *err;          // device status word: set when a bounded wait gives up
+  void *status;      // chained scan: look-back slots (ChainSlot), a power of two
+  uint64_t status_mask;
+  uint64_t gid_base;  // unit id of this launch's first chunk
 };
+// One look-back slot of the chained scan: flag = (unit id << 2) | state
+// (1 aggregate, 2 inclusive prefix); values are the accumulator's bits.
+struct alignas(32) ChainSlot {
+  unsigned long long flag, agg, incl, pad;
+};
+// elements per chunk of the chained scan for an input type (0: not used)
+int64_t scan_chain_chunk(int dop, int in_dt, int f32_comp);
 pdlgb300_error launch_cumusum(int dop, int in_dt, ScanArgs g, cudaStream_t s);
 size_t scan_acc_size(int dop, int in_dt, int f32_comp);
 

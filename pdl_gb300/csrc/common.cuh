@@ -114,6 +114,14 @@ template <class T> __host__ __device__ inline bool isnan_any(T v) {
   if constexpr (std::is_floating_point_v<T>) return v != v; else return false;
 }
 
+// Bad-value test with the mode fixed at compile time: BM 0 = no bad values,
+// 1 = the badvalue compares equal, 2 = the badvalue is NaN.
+template <class In, int BM> __device__ __forceinline__ bool is_bad(In v, In bad) {
+  if constexpr (BM == 0) return false;
+  else if constexpr (BM == 2) return isnan_any(v);
+  else return v == bad;
+}
+
 // ------------------------------------------------------------ loop plans
 
 // A broadcast loop after collapsing: nd dims (innermost first) with sizes

@@ -82,7 +82,8 @@ template <class In, class Out, bool COMP> struct SumAcc {
 template <class In, class Out, bool COMP> struct OpSum {
   using S = SumAcc<In, Out, COMP>;
   using Acc = typename S::Acc;
-  static constexpr bool kCount = false, kVec = true;
+  static constexpr bool kCount = false, kVec = true, kNeutral = true;
+  __device__ static In neutral() { return (In)0; }
   static constexpr bool kBlock = std::is_same_v<Acc, F64Sum>;
   static constexpr int kU = kBlock ? 8 : 0;
   template <int VEC, int U>
@@ -107,7 +108,8 @@ template <class In, class Out, bool COMP> struct OpSum {
 
 template <class In, class Out> struct OpProd {
   using Acc = std::conditional_t<std::is_integral_v<Out>, uns_t<Out>, Out>;
-  static constexpr bool kCount = false, kVec = true, kBlock = false;
+  static constexpr bool kCount = false, kVec = true, kBlock = false, kNeutral = true;
+  __device__ static In neutral() { return (In)1; }
   static constexpr int kU = 0;
   template <int VEC, int U>
   __device__ static void add_block(Acc &, const In *, int64_t, int64_t) {}
@@ -133,7 +135,8 @@ template <class In, class Out> struct OpProd {
 template <class In, class Out, bool COMP> struct OpAvg {
   using S = SumAcc<In, Out, COMP>;
   using Acc = typename S::Acc;
-  static constexpr bool kCount = true, kVec = true;
+  static constexpr bool kCount = true, kVec = true, kNeutral = true;
+  __device__ static In neutral() { return (In)0; }
   static constexpr bool kBlock = std::is_same_v<Acc, F64Sum>;
   static constexpr int kU = kBlock ? 8 : 0;
   template <int VEC, int U>
@@ -178,7 +181,8 @@ template <class T> struct MMAcc {
 template <class T, bool MAX, bool IND> struct OpMM {
   using Acc = MMAcc<T>;
   using Out = std::conditional_t<IND, int64_t, T>;
-  static constexpr bool kCount = false, kVec = true, kBlock = false;
+  static constexpr bool kCount = false, kVec = true, kBlock = false, kNeutral = false;
+  __device__ static T neutral() { return (T)0; }
   static constexpr int kU = 0;
   template <int VEC, int U>
   __device__ static void add_block(Acc &, const T *, int64_t, int64_t) {}
@@ -233,7 +237,8 @@ template <bool MAX, bool IND> struct OpMM<double, MAX, IND> {
     uint64_t bits;
   };
   using Out = std::conditional_t<IND, int64_t, double>;
-  static constexpr bool kCount = false, kVec = true, kBlock = true;
+  static constexpr bool kCount = false, kVec = true, kBlock = true, kNeutral = false;
+  __device__ static double neutral() { return 0.0; }
   static constexpr int kU = 8;
   __device__ static int64_t key_of(uint64_t b) {
     if ((b & 0x7FFFFFFFFFFFFFFFull) > 0x7FF0000000000000ull) return KEY_NAN;
@@ -368,72 +373,80 @@ template <class V> __device__ __forceinline__ V ldv(const V *p) {
 }
 
 // Accumulate elements [lo, hi) of a contiguous row, G threads, lane `lane`.
-template <class Op, class In, bool BAD>
+// Ops with a neutral element (sums, products) add it in place of a bad
+// value, so the inner loop has no branches; the good count is the range
+// size (added by lane 0) minus each lane's bad count.
+template <class Op, class In, int BM>
 __device__ __forceinline__ void row_accumulate(const In *row, int64_t lo, int64_t hi,
-                                               int lane, int G, const Bad<In> &bv,
+                                               int lane, int G, In bad,
                                                AccCnt<typename Op::Acc> &ac) {
   constexpr int VEC = 16 / sizeof(In);
   constexpr int U = Op::kU ? Op::kU : 8;  // 16-byte vectors in flight per thread
-  int64_t i = lo;
+  uint32_t nb = 0;
+  auto take = [&](In v, int64_t idx, uint32_t &cnt) {
+    if constexpr (BM == 0) {
+      Op::add(ac.acc, v, idx);
+    } else {
+      const bool b = is_bad<In, BM>(v, bad);
+      cnt += b;
+      if constexpr (Op::kNeutral) Op::add(ac.acc, b ? Op::neutral() : v, idx);
+      else if (!b) Op::add(ac.acc, v, idx);
+    }
+  };
   // scalar head up to a 16-byte boundary
   int64_t mis = ((uintptr_t)(row + lo) & 15) / sizeof(In);
   int64_t head = mis ? (VEC - mis) : 0;
   if (head > hi - lo) head = hi - lo;
-  if (lane < head) {
-    In v = row[lo + lane];
-    if (!(BAD && bv.is(v))) {
-      Op::add(ac.acc, v, lo + lane);
-      ac.cnt++;
+  if (lane < head) take(row[lo + lane], lo + lane, nb);
+  const int64_t i = lo + head;
+  const VecT<In, VEC> *vp = reinterpret_cast<const VecT<In, VEC> *>(row + i);
+  const int64_t nv = (hi - i) / VEC;
+  const int64_t per = (int64_t)G * U;
+  int64_t nbad = 0;
+  int64_t k = lane;
+  // full iterations: all U vectors in range, no per-vector checks
+  for (; k + (int64_t)(U - 1) * G < nv; k += per) {
+    VecT<In, VEC> buf[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) buf[u] = ldv(vp + k + (int64_t)u * G);
+    if constexpr (BM == 0 && Op::kBlock) {
+      Op::template add_block<VEC, U>(ac.acc, reinterpret_cast<const In *>(buf), i + k * VEC,
+                                     (int64_t)G * VEC);
+    } else {
+      uint32_t nbi = 0;
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        const int64_t base = i + (k + (int64_t)u * G) * VEC;
+        if constexpr (BM == 0) {
+          Op::template add_vec<VEC>(ac.acc, buf[u].e, base);
+        } else {
+#pragma unroll
+          for (int e = 0; e < VEC; e++) take(buf[u].e[e], base + e, nbi);
+        }
+      }
+      nbad += nbi;
     }
   }
-  i = lo + head;
-  const VecT<In, VEC> *vp = reinterpret_cast<const VecT<In, VEC> *>(row + i);
-  int64_t nv = (hi - i) / VEC;
-  for (int64_t k = lane; k < nv; k += (int64_t)G * U) {
-    VecT<In, VEC> buf[U];
-    const bool full = k + (int64_t)(U - 1) * G < nv;
+  // the last, partial iteration
+  if (k < nv) {
 #pragma unroll
     for (int u = 0; u < U; u++) {
-      int64_t kk = k + (int64_t)u * G;
-      if (full || kk < nv) buf[u] = ldv(vp + kk);
-    }
-    if constexpr (!BAD && Op::kBlock) {
-      if (full) {
-        Op::template add_block<VEC, U>(ac.acc, reinterpret_cast<const In *>(buf),
-                                       i + k * VEC, (int64_t)G * VEC);
-        if constexpr (Op::kCount) ac.cnt += VEC * U;
-        continue;
-      }
-    }
-#pragma unroll
-    for (int u = 0; u < U; u++) {
-      int64_t kk = k + (int64_t)u * G;
-      if (full || kk < nv) {
-        int64_t base = i + kk * VEC;
-        if constexpr (BAD) {
-#pragma unroll
-          for (int e = 0; e < VEC; e++) {
-            In v = buf[u].e[e];
-            if (!bv.is(v)) {
-              Op::add(ac.acc, v, base + e);
-              ac.cnt++;
-            }
-          }
+      const int64_t kk = k + (int64_t)u * G;
+      if (kk < nv) {
+        VecT<In, VEC> v = ldv(vp + kk);
+        const int64_t base = i + kk * VEC;
+        if constexpr (BM == 0) {
+          Op::template add_vec<VEC>(ac.acc, v.e, base);
         } else {
-          Op::template add_vec<VEC>(ac.acc, buf[u].e, base);
-          if constexpr (Op::kCount) ac.cnt += VEC;
+#pragma unroll
+          for (int e = 0; e < VEC; e++) take(v.e[e], base + e, nb);
         }
       }
     }
   }
   // scalar tail
-  for (int64_t t = i + nv * VEC + lane; t < hi; t += G) {
-    In v = row[t];
-    if (!(BAD && bv.is(v))) {
-      Op::add(ac.acc, v, t);
-      ac.cnt++;
-    }
-  }
+  for (int64_t t = i + nv * VEC + lane; t < hi; t += G) take(row[t], t, nb);
+  ac.cnt += (lane == 0 ? hi - lo : 0) - nbad - (int64_t)nb;
 }
 
 // Accumulate elements [lo, hi) of a strided row (scalar loads).
@@ -484,9 +497,16 @@ __global__ void __launch_bounds__(512) k_red_rows(const RedArgs args) {
       if (lo > hi) lo = hi;
     }
     AC ac{Op::init(), 0};
-    if (args.inc_n == 1)
-      row_accumulate<Op, In, BAD>(a, lo, hi, lane, G, bv, ac);
-    else
+    if (args.inc_n == 1) {
+      if constexpr (!BAD) {
+        row_accumulate<Op, In, 0>(a, lo, hi, lane, G, bv.val, ac);
+      } else if constexpr (std::is_floating_point_v<In>) {
+        if (bv.isnan_) row_accumulate<Op, In, 2>(a, lo, hi, lane, G, bv.val, ac);
+        else row_accumulate<Op, In, 1>(a, lo, hi, lane, G, bv.val, ac);
+      } else {
+        row_accumulate<Op, In, 1>(a, lo, hi, lane, G, bv.val, ac);
+      }
+    } else
       row_accumulate_strided<Op, In, BAD>(a, args.inc_n, lo, hi, lane, G, bv, ac);
     ac = group_reduce<Op>(ac, G);
     if (lane == 0) {
@@ -502,25 +522,33 @@ __global__ void __launch_bounds__(512) k_red_rows(const RedArgs args) {
   }
 }
 
-// Combine the per-split partials of each row, in split order.
+// Combine the per-split partials of each row: one warp per row, each lane
+// merging every 32nd split, then a shuffle tree (min/max ties are settled by
+// index inside merge, so the order of the merges does not matter for them).
 template <class Op, class In, class Out, bool BAD>
 __global__ void k_red_combine(const RedArgs args) {
   using Acc = typename Op::Acc;
+  using AC = AccCnt<Acc>;
   Out obad = from_bits<Out>(args.bbad_bits);
-  for (int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; row < args.rows;
-       row += (int64_t)gridDim.x * blockDim.x) {
+  const int lane = threadIdx.x & 31;
+  const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t row = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+       row < args.rows; row += nw) {
     const Acc *p = reinterpret_cast<const Acc *>(args.partials) + row * args.nsplit;
-    Acc acc = p[0];
-    int64_t cnt = args.pcounts[row * args.nsplit];
-    for (int s = 1; s < args.nsplit; s++) {
-      Op::merge(acc, p[s]);
-      cnt += args.pcounts[row * args.nsplit + s];
+    const int64_t *pc = args.pcounts + row * args.nsplit;
+    AC ac{Op::init(), 0};
+    for (int s = lane; s < args.nsplit; s += 32) {
+      AC o{p[s], pc[s]};
+      merge_ac<Op>(ac, o);
     }
-    int64_t offs[MAXP];
-    loop_offsets(args.L, row, offs);
-    if (!(BAD || Op::kCount || args.inc_n != 1)) cnt = args.n;
-    Out r = Op::fin(acc, cnt, BAD, obad, args.setbad);
-    store_out<Out>(args.b + offs[1] * (int64_t)sizeof(Out), r);
+    ac = group_reduce<Op>(ac, 32);
+    if (lane == 0) {
+      int64_t offs[MAXP];
+      loop_offsets(args.L, row, offs);
+      const int64_t cnt = (BAD || Op::kCount || args.inc_n != 1) ? ac.cnt : args.n;
+      Out r = Op::fin(ac.acc, cnt, BAD, obad, args.setbad);
+      store_out<Out>(args.b + offs[1] * (int64_t)sizeof(Out), r);
+    }
   }
 }
 
@@ -563,7 +591,7 @@ pdlgb300_error launch_red_typed(RedArgs args, const RedLaunch &lc, cudaStream_t 
     if (args.nsplit > 1) {
       if (!pgh::cuda_check(cudaGetLastError(), &e, nm)) return e;
       pgh::record_kernel(nm, lc.grid, lc.block);
-      int g = (int)std::min<int64_t>((args.rows + 127) / 128, 65535);
+      int g = (int)std::min<int64_t>((args.rows + 3) / 4, 65535);
       if (args.bad) k_red_combine<Op, In, Out, true><<<g, 128, 0, s>>>(args);
       else k_red_combine<Op, In, Out, false><<<g, 128, 0, s>>>(args);
       nm = "k_red_combine";

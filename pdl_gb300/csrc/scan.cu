@@ -210,6 +210,274 @@ __global__ void __launch_bounds__(256) k_scan_warp(const ScanArgs g) {
   }
 }
 
+// ----------------------------------------------------------- chained scan
+// Contiguous, 16-byte aligned rows of 4- and 8-byte types: one block per
+// chunk of 32 KiB of input (8192 float32 / 4096 float64), each thread owning
+// 128 contiguous bytes.  Loads are striped 16-byte cp.async copies into a
+// shared-memory tile whose 16-byte slots are XOR-swizzled by lane, so both
+// the striped copies and each thread's blocked reads are free of bank
+// conflicts; outputs go back the same way and leave as coalesced 16-byte
+// stores.  Inside the chunk: thread totals, a warp scan, a block scan.
+// Across the chunks of a row the carry travels by decoupled look-back:
+// each chunk publishes its total (A), then its inclusive prefix (P), in a
+// slot tagged with a 64-bit unit id (no reset between launches); a chunk
+// reads up to 128 predecessors per round and stops at the nearest P.
+// Chunks are taken in blockIdx order, so a chunk only waits on chunks whose
+// blocks were dispatched before it.  Every wait is bounded: on timeout the
+// status word gets bit 4 and the chunk goes on with what it has.
+constexpr int CB = 256;  // threads per chained-scan block
+constexpr int LB_PER_LANE = 4;  // look-back slots read per lane per round
+
+__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long *p) {
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long *p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_u64(unsigned long long *p, unsigned long long v) {
+  asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ void st_relaxed_u64(unsigned long long *p, unsigned long long v) {
+  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+template <class A> __device__ __forceinline__ unsigned long long acc_to_u64(A a) {
+  static_assert(sizeof(A) <= 8, "look-back values are at most 8 bytes");
+  unsigned long long u = 0;
+  memcpy(&u, &a, sizeof a);
+  return u;
+}
+template <class A> __device__ __forceinline__ A u64_to_acc(unsigned long long u) {
+  A a;
+  memcpy(&a, &u, sizeof a);
+  return a;
+}
+
+// state 1: aggregate only, 2: inclusive prefix
+__device__ __forceinline__ void chain_publish(ChainSlot *sl, uint64_t gid, int state,
+                                              unsigned long long v) {
+  st_relaxed_u64(state == 2 ? &sl->incl : &sl->agg, v);
+  st_release_u64(&sl->flag, (gid << 2) | (uint64_t)state);
+}
+
+template <class In, class Out, int BM, bool COMP>
+__global__ void __launch_bounds__(CB, 4) k_scan_chain(const ScanArgs g, int64_t u0) {
+  using S = ScanT<In, Out, COMP>;
+  using Acc = typename S::Acc;
+  constexpr int ITEMS = 128 / sizeof(In);                // per thread
+  constexpr int VEC = 16 / sizeof(In);
+  constexpr int NV = ITEMS / VEC;                        // 8 input vectors per thread
+  constexpr int VO = 16 / sizeof(Out);                   // outputs per 16-byte vector
+  constexpr int OV = ITEMS / VO;                         // output vectors per thread
+  constexpr int WSPAN = 32 * ITEMS;                      // elements per warp
+  constexpr int CH = (CB / 32) * WSPAN;                  // elements per chunk
+  static_assert(NV == 8 && (OV == 8 || OV == 16), "swizzle needs 8 or 16 slots per row");
+  extern __shared__ __align__(16) unsigned char sm_tile[];
+  __shared__ Acc s_w[CB / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  unsigned char *wbuf = sm_tile + (size_t)warp * 32 * OV * 16;
+  const uint32_t sb = (uint32_t)__cvta_generic_to_shared(wbuf);
+  const int64_t u = u0 + blockIdx.x;
+  const int64_t row = u / g.nchunk;
+  const int c = (int)(u - row * g.nchunk);
+  int64_t offs[MAXP];
+  loop_offsets(g.L, row, offs);
+  const In *a = reinterpret_cast<const In *>(g.a) + offs[0];
+  Out *b = reinterpret_cast<Out *>(g.b) + offs[1];
+  const int64_t lo = (int64_t)c * CH;
+  const int64_t hi = lo + CH < g.n ? lo + CH : g.n;
+  const int64_t wlo = lo + (int64_t)warp * WSPAN;
+  const bool fast = wlo + WSPAN <= hi;
+  const In bad = from_bits<In>(g.abad);
+  const Out obad = from_bits<Out>(g.bbad);
+  int nvalid = ITEMS;  // items of this thread inside the row
+  In v[ITEMS];
+  if (fast) {
+#pragma unroll
+    for (int r = 0; r < NV; r++) {
+      const int gv = r * 32 + lane;  // 16-byte vector of the warp's span
+      const int own = gv / NV, q = gv % NV;
+      const uint32_t dst = sb + (uint32_t)(own * NV * 16 + ((q ^ (own & 7)) * 16));
+      asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst),
+                   "l"(a + wlo + (int64_t)gv * VEC)
+                   : "memory");
+    }
+    asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;" ::: "memory");
+    __syncwarp();
+#pragma unroll
+    for (int q = 0; q < NV; q++) {
+      float4 f;
+      const uint32_t src = sb + (uint32_t)(lane * NV * 16 + ((q ^ (lane & 7)) * 16));
+      asm volatile("ld.shared.v4.f32 {%0,%1,%2,%3}, [%4];"
+                   : "=f"(f.x), "=f"(f.y), "=f"(f.z), "=f"(f.w)
+                   : "r"(src));
+      memcpy(&v[q * VEC], &f, 16);
+    }
+  } else {
+    const int64_t t0 = wlo + (int64_t)lane * ITEMS;
+    const int64_t left = hi - t0;
+    nvalid = left <= 0 ? 0 : (left >= ITEMS ? ITEMS : (int)left);
+#pragma unroll
+    for (int j = 0; j < ITEMS; j++) v[j] = j < nvalid ? a[t0 + j] : (In)0;
+  }
+  // items past the row's end hold 0, which adds nothing and is never stored
+  auto good = [&](int j) { return !is_bad<In, BM>(v[j], bad); };
+
+  // thread total
+  Acc tot = S::zero();
+  if constexpr (std::is_same_v<In, double> && std::is_same_v<Out, double>) {
+    double w[ITEMS];
+#pragma unroll
+    for (int j = 0; j < ITEMS; j++) w[j] = good(j) ? v[j] : 0.0;
+    F64Sum fs{0.0};
+    fs.add_block<ITEMS>(w);
+    tot = fs.s;
+  } else {
+#pragma unroll
+    for (int j = 0; j < ITEMS; j++)
+      if (good(j)) tot = S::add1(tot, v[j]);
+  }
+  // warp scan of the thread totals
+  Acc inc = tot;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    Acc o = shfl_up_any(inc, d);
+    if (lane >= d) inc = S::add(o, inc);
+  }
+  Acc lex = shfl_up_any(inc, 1);
+  if (lane == 0) lex = S::zero();
+  if (lane == 31) s_w[warp] = inc;
+  __syncthreads();
+  if (warp == 0) {
+    constexpr int NW = CB / 32;
+    Acc wt = lane < NW ? s_w[lane] : S::zero();
+#pragma unroll
+    for (int d = 1; d < NW; d <<= 1) {
+      Acc o = shfl_up_any(wt, d);
+      if (lane >= d) wt = S::add(o, wt);
+    }
+    const Acc agg = shfl_any(wt, NW - 1);
+    Acc wex = shfl_up_any(wt, 1);
+    if (lane == 0) wex = S::zero();
+    Acc excl = S::zero();
+    if (g.nchunk > 1) {
+      ChainSlot *slots = reinterpret_cast<ChainSlot *>(g.status);
+      const uint64_t gid = g.gid_base + (uint64_t)u;
+      if (c == 0) {
+        if (lane == 0) chain_publish(&slots[gid & g.status_mask], gid, 2, acc_to_u64(agg));
+      } else {
+        if (lane == 0) chain_publish(&slots[gid & g.status_mask], gid, 1, acc_to_u64(agg));
+        const uint64_t gid0 = gid - (uint64_t)c;  // the row's chunk 0
+        int64_t pos = c - 1;                      // newest predecessor not yet added
+        constexpr int WIN = 32 * LB_PER_LANE;
+        while (true) {
+          int st[LB_PER_LANE];
+          unsigned long long val[LB_PER_LANE];
+          int kp = 1 << 30;
+#pragma unroll
+          for (int qq = 0; qq < LB_PER_LANE; qq++) {
+            const int k = lane * LB_PER_LANE + qq;
+            const int64_t p = pos - k;
+            st[qq] = 3;  // before the row's start: nothing to add, stop here
+            val[qq] = 0;
+            if (p >= 0) {
+              const uint64_t gp = gid0 + (uint64_t)p;
+              ChainSlot *sl = &slots[gp & g.status_mask];
+              unsigned long long f = 0;
+              int spins = 0;
+              while (true) {
+                f = ld_acquire_u64(&sl->flag);
+                if ((f >> 2) == gp && (f & 3)) break;
+                if (++spins > (1 << 21)) {
+                  atomicOr(g.err, 4);
+                  f = (gp << 2) | 3;
+                  break;
+                }
+                __nanosleep(32);
+              }
+              st[qq] = (int)(f & 3);
+              if (st[qq] == 1) val[qq] = ld_relaxed_u64(&sl->agg);
+              else if (st[qq] == 2) val[qq] = ld_relaxed_u64(&sl->incl);
+            }
+            if (st[qq] >= 2 && k < kp) kp = k;
+          }
+          __syncwarp();
+          const int kmin = __reduce_min_sync(0xffffffffu, kp);
+          Acc part = S::zero();
+#pragma unroll
+          for (int qq = LB_PER_LANE - 1; qq >= 0; qq--) {
+            const int k = lane * LB_PER_LANE + qq;
+            if (k <= kmin && st[qq] != 3) part = S::add(part, u64_to_acc<Acc>(val[qq]));
+          }
+#pragma unroll
+          for (int d = 16; d > 0; d >>= 1) part = S::add(shfl_down_any2(part, d), part);
+          part = shfl_any(part, 0);
+          excl = S::add(part, excl);
+          if (kmin < WIN) break;
+          pos -= WIN;
+        }
+        if (lane == 0)
+          chain_publish(&slots[gid & g.status_mask], gid, 2, acc_to_u64(S::add(excl, agg)));
+      }
+    }
+    if (lane < NW) s_w[lane] = S::add(excl, wex);
+  }
+  __syncthreads();
+  Acc run = S::add(s_w[warp], lex);
+
+  // running sums, staged in the swizzled tile
+  if (fast) {
+#pragma unroll
+    for (int pv = 0; pv < OV; pv++) {
+      Out o[VO];
+#pragma unroll
+      for (int e = 0; e < VO; e++) {
+        const int j = pv * VO + e;
+        if (good(j)) {
+          run = S::add1(run, v[j]);
+          o[e] = S::value(run);
+        } else {
+          o[e] = obad;
+        }
+      }
+      float4 f;
+      memcpy(&f, o, 16);
+      const uint32_t dst = sb + (uint32_t)(lane * OV * 16 + ((pv ^ (lane & 7)) * 16));
+      asm volatile("st.shared.v4.f32 [%0], {%1,%2,%3,%4};" ::"r"(dst), "f"(f.x), "f"(f.y),
+                   "f"(f.z), "f"(f.w)
+                   : "memory");
+    }
+    __syncwarp();
+#pragma unroll
+    for (int r = 0; r < OV; r++) {
+      const int gv = r * 32 + lane;
+      const int own = gv / OV, pv = gv % OV;
+      const uint32_t src = sb + (uint32_t)(own * OV * 16 + ((pv ^ (own & 7)) * 16));
+      float4 f;
+      asm volatile("ld.shared.v4.f32 {%0,%1,%2,%3}, [%4];"
+                   : "=f"(f.x), "=f"(f.y), "=f"(f.z), "=f"(f.w)
+                   : "r"(src));
+      __stcs(reinterpret_cast<float4 *>(b + wlo + (int64_t)gv * VO), f);
+    }
+  } else {
+    const int64_t t0 = wlo + (int64_t)lane * ITEMS;
+#pragma unroll
+    for (int j = 0; j < ITEMS; j++) {
+      if (j < nvalid) {
+        Out o = obad;
+        if (good(j)) {
+          run = S::add1(run, v[j]);
+          o = S::value(run);
+        }
+        b[t0 + j] = o;
+      }
+    }
+  }
+}
+
 // One thread per row, any increments, the reference's order.
 template <class In, class Out, bool BAD, bool COMP>
 __global__ void k_scan_thread(const ScanArgs g) {
@@ -235,10 +503,52 @@ __global__ void k_scan_thread(const ScanArgs g) {
   }
 }
 
+template <class In, class Out> constexpr bool chain_ok() {
+  return (sizeof(In) == 4 || sizeof(In) == 8) &&
+         (sizeof(Out) == sizeof(In) || sizeof(Out) == 2 * sizeof(In));
+}
+
+template <class In, class Out, bool COMP>
+pdlgb300_error scan_chain_typed(ScanArgs g, cudaStream_t s) {
+  pdlgb300_error e = pgh::ok();
+  if constexpr (chain_ok<In, Out>()) {
+    constexpr int ITEMS = 128 / sizeof(In);
+    constexpr size_t smem = (size_t)CB * ITEMS * sizeof(Out);
+    static bool attr = false;
+    if (!attr) {
+      cudaFuncSetAttribute(k_scan_chain<In, Out, 0, COMP>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      cudaFuncSetAttribute(k_scan_chain<In, Out, 1, COMP>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      cudaFuncSetAttribute(k_scan_chain<In, Out, 2, COMP>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      attr = true;
+    }
+    const int64_t units = g.rows * g.nchunk;
+    for (int64_t u0 = 0; u0 < units; u0 += (int64_t)1 << 30) {
+      const int grid = (int)std::min<int64_t>(units - u0, (int64_t)1 << 30);
+      if (!g.bad) k_scan_chain<In, Out, 0, COMP><<<grid, CB, smem, s>>>(g, u0);
+      else if (g.abad_isnan) k_scan_chain<In, Out, 2, COMP><<<grid, CB, smem, s>>>(g, u0);
+      else k_scan_chain<In, Out, 1, COMP><<<grid, CB, smem, s>>>(g, u0);
+      if (!pgh::cuda_check(cudaGetLastError(), &e, "k_scan_chain")) return e;
+      pgh::record_kernel("k_scan_chain", grid, CB);
+    }
+  } else {
+    e = pgh::err(PDLGB300_EFATAL, "chained scan: unsupported type pair");
+  }
+  return e;
+}
+
+template <class In, class Out> constexpr int64_t chain_chunk() {
+  if constexpr (chain_ok<In, Out>()) return (int64_t)CB * (128 / sizeof(In));
+  return 0;
+}
+
 template <class In, class Out, bool COMP>
 pdlgb300_error scan_typed(ScanArgs g, cudaStream_t s) {
   pdlgb300_error e = pgh::ok();
   if (g.rows == 0) return e;
+  if (g.status || g.mode == 3) return scan_chain_typed<In, Out, COMP>(g, s);
   const int nsm = pgh::num_sms();
   if (g.mode < 0) {  // thread kernel
     int64_t grid = std::min<int64_t>((g.rows + 127) / 128, (int64_t)nsm * 32);
@@ -284,6 +594,18 @@ pdlgb300_error launch_cumusum(int dop, int in_dt, ScanArgs g, cudaStream_t s) {
     return scan_typed<In, OutP, false>(g, s);
   });
   return pgh::err(PDLGB300_EUSERERROR, "cumusumover: unsupported type %d", in_dt);
+}
+
+int64_t scan_chain_chunk(int dop, int in_dt, int comp) {
+  int64_t r = 0;
+  PG_DISPATCH(in_dt, {
+    using In = typename TT<DT>::T;
+    using OutP = typename TT<intplus(DT)>::T;
+    (void)comp;
+    if (dop == 1) r = chain_chunk<In, double>();
+    else r = chain_chunk<In, OutP>();
+  });
+  return r;
 }
 
 size_t scan_acc_size(int dop, int in_dt, int comp) {

@@ -345,3 +345,48 @@ def test_convert_matches_c_casts(gpu, src):
         else:
             want = a.astype(NP_DTYPES[type_code(dst)])
         assert np.array_equal(got, want), (src, dst)
+
+
+@pytest.mark.parametrize("t,n,rows", [("float", (1 << 21) + 123, 1), ("float", 9004, 5),
+                                      ("double", 300_007, 2), ("long", 3 * 8192 + 4, 3),
+                                      ("longlong", 70_000, 2), ("float", 65536, 40)])
+@pytest.mark.parametrize("op", ["cumusumover", "dcumusumover"])
+def test_chained_scan_rows(gpu, op, t, n, rows):
+    """Contiguous aligned rows of 4/8-byte types run the chained single-pass
+    scan: several chunks per row (look-back inside the row), a row of 257
+    chunks (three look-back rounds of 128), ragged last chunks."""
+    rng = seeded(n + rows)
+    a, _ = rand_array(rng, t, (rows, n), -10, 10)
+    x = to_pdl(a, t)
+    got, exp = _run_both(op, [x])
+    rtol, atol, scale = _tol(op, a, exp, exp.type) if exp.type in FLOAT_TYPES else (0, 0, None)
+    assert_same(got, exp, rtol=rtol, atol=atol, scale=scale, what=f"{op} {t} {rows}x{n}")
+
+
+@pytest.mark.parametrize("t", ["float", "double", "long"])
+@pytest.mark.parametrize("nanbad", [False, True])
+def test_chained_scan_bad_values(gpu, t, nanbad):
+    rng = seeded(21)
+    a, bad = rand_array(rng, t, (3, 50_000), -10, 10, bad_frac=0.05)
+    x = to_pdl(a, t, badflag=True)
+    if nanbad:
+        if t == "long":
+            pytest.skip("NaN badvalue is for float types")
+        arr = x.numpy().copy()
+        arr[bad] = np.nan
+        x = to_pdl(arr, t, badflag=True)
+        x.badvalue(float("nan"))
+    got, exp = _run_both("cumusumover", [x])
+    clean = np.where(bad, 0, a)
+    rtol, atol, scale = _tol("cumusumover", clean, exp, exp.type) if exp.type in FLOAT_TYPES else (0, 0, None)
+    assert_same(got, exp, rtol=rtol, atol=atol, scale=scale, what=f"cumusumover {t} bad nan={nanbad}")
+
+
+def test_chained_scan_unaligned_rows_fall_back(gpu):
+    """Rows whose starts are not 16-byte aligned take the warp kernel."""
+    rng = seeded(22)
+    a, _ = rand_array(rng, "float", (4, 20_001), -10, 10)
+    x = to_pdl(a, "float").slice(slice(1, None))
+    got, exp = _run_both("cumusumover", [x])
+    rtol, atol, scale = _tol("cumusumover", x.numpy(), exp, exp.type)
+    assert_same(got, exp, rtol=rtol, atol=atol, scale=scale, what="cumusumover unaligned")
