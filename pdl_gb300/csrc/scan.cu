@@ -263,8 +263,72 @@ __device__ __forceinline__ void chain_publish(ChainSlot *sl, uint64_t gid, int s
   st_release_u64(&sl->flag, (gid << 2) | (uint64_t)state);
 }
 
+// Look-back of chunk c > 0 of a row (warp 0): the sum of its predecessors'
+// values up to the nearest inclusive prefix.  gid is the chunk's unit id.
+template <class S, class Acc>
+__device__ __forceinline__ Acc chain_lookback(const ScanArgs &g, ChainSlot *slots, uint64_t gid,
+                                              int c, int lane) {
+  Acc excl = S::zero();
+  const uint64_t gid0 = gid - (uint64_t)c;  // the row's chunk 0
+  int64_t pos = c - 1;                      // newest predecessor not yet added
+  constexpr int WIN = 32 * LB_PER_LANE;
+  while (true) {
+    int st[LB_PER_LANE];
+    unsigned long long val[LB_PER_LANE];
+    int kp = 1 << 30;
+#pragma unroll
+    for (int qq = 0; qq < LB_PER_LANE; qq++) {
+      const int k = lane * LB_PER_LANE + qq;
+      const int64_t p = pos - k;
+      st[qq] = 3;  // before the row's start: nothing to add, stop here
+      val[qq] = 0;
+      if (p >= 0) {
+        const uint64_t gp = gid0 + (uint64_t)p;
+        ChainSlot *sl = &slots[gp & g.status_mask];
+        unsigned long long f = 0;
+        int spins = 0;
+        while (true) {
+          f = ld_acquire_u64(&sl->flag);
+          if ((f >> 2) == gp && (f & 3)) break;
+          if (++spins > (1 << 21)) {
+            atomicOr(g.err, 4);
+            f = (gp << 2) | 3;
+            break;
+          }
+          __nanosleep(32);
+        }
+        st[qq] = (int)(f & 3);
+        if (st[qq] == 1) val[qq] = ld_relaxed_u64(&sl->agg);
+        else if (st[qq] == 2) val[qq] = ld_relaxed_u64(&sl->incl);
+      }
+      if (st[qq] >= 2 && k < kp) kp = k;
+    }
+    __syncwarp();
+    const int kmin = __reduce_min_sync(0xffffffffu, kp);
+    Acc part = S::zero();
+#pragma unroll
+    for (int qq = LB_PER_LANE - 1; qq >= 0; qq--) {
+      const int k = lane * LB_PER_LANE + qq;
+      if (k <= kmin && st[qq] != 3) part = S::add(part, u64_to_acc<Acc>(val[qq]));
+    }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) part = S::add(shfl_down_any2(part, d), part);
+    part = shfl_any(part, 0);
+    excl = S::add(part, excl);
+    if (kmin < WIN) break;
+    pos -= WIN;
+  }
+  return excl;
+}
+
+// The chunk's input stays in the swizzled tile (read once for the thread
+// totals, once for the running sums), so a thread holds no input registers
+// across the block barriers and more blocks fit on an SM to cover the
+// look-back latency.  Equal-width outputs overwrite their input slots; wider
+// outputs (float32 -> float64) use a second, larger tile.
 template <class In, class Out, int BM, bool COMP>
-__global__ void __launch_bounds__(CB, 4) k_scan_chain(const ScanArgs g, int64_t u0) {
+__global__ void __launch_bounds__(CB, sizeof(In) == 4 && sizeof(Out) == 4 ? 6 : 4)
+    k_scan_chain(const ScanArgs g, int64_t u0) {
   using S = ScanT<In, Out, COMP>;
   using Acc = typename S::Acc;
   constexpr int ITEMS = 128 / sizeof(In);                // per thread
@@ -274,71 +338,96 @@ __global__ void __launch_bounds__(CB, 4) k_scan_chain(const ScanArgs g, int64_t 
   constexpr int OV = ITEMS / VO;                         // output vectors per thread
   constexpr int WSPAN = 32 * ITEMS;                      // elements per warp
   constexpr int CH = (CB / 32) * WSPAN;                  // elements per chunk
+  constexpr int WIN_B = 32 * NV * 16;                    // input tile bytes per warp
+  constexpr int WOUT_B = OV == NV ? 0 : 32 * OV * 16;    // separate output tile per warp
   static_assert(NV == 8 && (OV == 8 || OV == 16), "swizzle needs 8 or 16 slots per row");
   extern __shared__ __align__(16) unsigned char sm_tile[];
   __shared__ Acc s_w[CB / 32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  unsigned char *wbuf = sm_tile + (size_t)warp * 32 * OV * 16;
-  const uint32_t sb = (uint32_t)__cvta_generic_to_shared(wbuf);
+  const uint32_t sin = (uint32_t)__cvta_generic_to_shared(sm_tile) + (uint32_t)(warp * WIN_B);
+  const uint32_t sout = OV == NV ? sin
+                                 : (uint32_t)__cvta_generic_to_shared(sm_tile) +
+                                       (uint32_t)((CB / 32) * WIN_B + warp * WOUT_B);
   const int64_t u = u0 + blockIdx.x;
   const int64_t row = u / g.nchunk;
   const int c = (int)(u - row * g.nchunk);
   int64_t offs[MAXP];
   loop_offsets(g.L, row, offs);
   const In *a = reinterpret_cast<const In *>(g.a) + offs[0];
-  Out *b = reinterpret_cast<Out *>(g.b) + offs[1];
   const int64_t lo = (int64_t)c * CH;
   const int64_t hi = lo + CH < g.n ? lo + CH : g.n;
   const int64_t wlo = lo + (int64_t)warp * WSPAN;
   const bool fast = wlo + WSPAN <= hi;
   const In bad = from_bits<In>(g.abad);
-  const Out obad = from_bits<Out>(g.bbad);
-  int nvalid = ITEMS;  // items of this thread inside the row
-  In v[ITEMS];
+  auto slot_in = [&](int q) { return sin + (uint32_t)(lane * NV * 16 + ((q ^ (lane & 7)) * 16)); };
+  auto ldin = [&](int q, In (&x)[VEC]) {
+    float4 f;
+    asm volatile("ld.shared.v4.f32 {%0,%1,%2,%3}, [%4];"
+                 : "=f"(f.x), "=f"(f.y), "=f"(f.z), "=f"(f.w)
+                 : "r"(slot_in(q)));
+    memcpy(x, &f, 16);
+  };
+  int nvalid = ITEMS;  // items of this thread inside the row (slow path)
+  const int64_t t0 = wlo + (int64_t)lane * ITEMS;
   if (fast) {
+    // striped 16-byte copies: vector q of lane L lands in row L, slot q ^ (L & 7)
 #pragma unroll
     for (int r = 0; r < NV; r++) {
-      const int gv = r * 32 + lane;  // 16-byte vector of the warp's span
+      const int gv = r * 32 + lane;
       const int own = gv / NV, q = gv % NV;
-      const uint32_t dst = sb + (uint32_t)(own * NV * 16 + ((q ^ (own & 7)) * 16));
+      const uint32_t dst = sin + (uint32_t)(own * NV * 16 + ((q ^ (own & 7)) * 16));
       asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst),
                    "l"(a + wlo + (int64_t)gv * VEC)
                    : "memory");
     }
     asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;" ::: "memory");
     __syncwarp();
-#pragma unroll
-    for (int q = 0; q < NV; q++) {
-      float4 f;
-      const uint32_t src = sb + (uint32_t)(lane * NV * 16 + ((q ^ (lane & 7)) * 16));
-      asm volatile("ld.shared.v4.f32 {%0,%1,%2,%3}, [%4];"
-                   : "=f"(f.x), "=f"(f.y), "=f"(f.z), "=f"(f.w)
-                   : "r"(src));
-      memcpy(&v[q * VEC], &f, 16);
-    }
   } else {
-    const int64_t t0 = wlo + (int64_t)lane * ITEMS;
+    // the ragged end of a row: this thread's items, zero past the end
     const int64_t left = hi - t0;
     nvalid = left <= 0 ? 0 : (left >= ITEMS ? ITEMS : (int)left);
 #pragma unroll
-    for (int j = 0; j < ITEMS; j++) v[j] = j < nvalid ? a[t0 + j] : (In)0;
+    for (int q = 0; q < NV; q++) {
+      In x[VEC];
+#pragma unroll
+      for (int e = 0; e < VEC; e++) x[e] = q * VEC + e < nvalid ? a[t0 + q * VEC + e] : (In)0;
+      float4 f;
+      memcpy(&f, x, 16);
+      asm volatile("st.shared.v4.f32 [%0], {%1,%2,%3,%4};" ::"r"(slot_in(q)), "f"(f.x),
+                   "f"(f.y), "f"(f.z), "f"(f.w)
+                   : "memory");
+    }
   }
   // items past the row's end hold 0, which adds nothing and is never stored
-  auto good = [&](int j) { return !is_bad<In, BM>(v[j], bad); };
+  auto good = [&](In x) { return !is_bad<In, BM>(x, bad); };
 
   // thread total
   Acc tot = S::zero();
   if constexpr (std::is_same_v<In, double> && std::is_same_v<Out, double>) {
-    double w[ITEMS];
-#pragma unroll
-    for (int j = 0; j < ITEMS; j++) w[j] = good(j) ? v[j] : 0.0;
+    // float64: two exact 8-element blocks (integer alignment, one FP64 add each)
     F64Sum fs{0.0};
-    fs.add_block<ITEMS>(w);
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      double w[NV];
+#pragma unroll
+      for (int q = 0; q < NV / 2; q++) {
+        In x[VEC];
+        ldin(h * (NV / 2) + q, x);
+#pragma unroll
+        for (int e = 0; e < VEC; e++) w[q * VEC + e] = good(x[e]) ? x[e] : 0.0;
+      }
+      fs.add_block<NV>(w);
+    }
     tot = fs.s;
   } else {
 #pragma unroll
-    for (int j = 0; j < ITEMS; j++)
-      if (good(j)) tot = S::add1(tot, v[j]);
+    for (int q = 0; q < NV; q++) {
+      In x[VEC];
+      ldin(q, x);
+#pragma unroll
+      for (int e = 0; e < VEC; e++)
+        if (good(x[e])) tot = S::add1(tot, x[e]);
+    }
   }
   // warp scan of the thread totals
   Acc inc = tot;
@@ -370,55 +459,7 @@ __global__ void __launch_bounds__(CB, 4) k_scan_chain(const ScanArgs g, int64_t 
         if (lane == 0) chain_publish(&slots[gid & g.status_mask], gid, 2, acc_to_u64(agg));
       } else {
         if (lane == 0) chain_publish(&slots[gid & g.status_mask], gid, 1, acc_to_u64(agg));
-        const uint64_t gid0 = gid - (uint64_t)c;  // the row's chunk 0
-        int64_t pos = c - 1;                      // newest predecessor not yet added
-        constexpr int WIN = 32 * LB_PER_LANE;
-        while (true) {
-          int st[LB_PER_LANE];
-          unsigned long long val[LB_PER_LANE];
-          int kp = 1 << 30;
-#pragma unroll
-          for (int qq = 0; qq < LB_PER_LANE; qq++) {
-            const int k = lane * LB_PER_LANE + qq;
-            const int64_t p = pos - k;
-            st[qq] = 3;  // before the row's start: nothing to add, stop here
-            val[qq] = 0;
-            if (p >= 0) {
-              const uint64_t gp = gid0 + (uint64_t)p;
-              ChainSlot *sl = &slots[gp & g.status_mask];
-              unsigned long long f = 0;
-              int spins = 0;
-              while (true) {
-                f = ld_acquire_u64(&sl->flag);
-                if ((f >> 2) == gp && (f & 3)) break;
-                if (++spins > (1 << 21)) {
-                  atomicOr(g.err, 4);
-                  f = (gp << 2) | 3;
-                  break;
-                }
-                __nanosleep(32);
-              }
-              st[qq] = (int)(f & 3);
-              if (st[qq] == 1) val[qq] = ld_relaxed_u64(&sl->agg);
-              else if (st[qq] == 2) val[qq] = ld_relaxed_u64(&sl->incl);
-            }
-            if (st[qq] >= 2 && k < kp) kp = k;
-          }
-          __syncwarp();
-          const int kmin = __reduce_min_sync(0xffffffffu, kp);
-          Acc part = S::zero();
-#pragma unroll
-          for (int qq = LB_PER_LANE - 1; qq >= 0; qq--) {
-            const int k = lane * LB_PER_LANE + qq;
-            if (k <= kmin && st[qq] != 3) part = S::add(part, u64_to_acc<Acc>(val[qq]));
-          }
-#pragma unroll
-          for (int d = 16; d > 0; d >>= 1) part = S::add(shfl_down_any2(part, d), part);
-          part = shfl_any(part, 0);
-          excl = S::add(part, excl);
-          if (kmin < WIN) break;
-          pos -= WIN;
-        }
+        excl = chain_lookback<S, Acc>(g, slots, gid, c, lane);
         if (lane == 0)
           chain_publish(&slots[gid & g.status_mask], gid, 2, acc_to_u64(S::add(excl, agg)));
       }
@@ -428,34 +469,41 @@ __global__ void __launch_bounds__(CB, 4) k_scan_chain(const ScanArgs g, int64_t 
   __syncthreads();
   Acc run = S::add(s_w[warp], lex);
 
-  // running sums, staged in the swizzled tile
-  if (fast) {
+  // running sums: read a vector, write its outputs (in place when as wide)
+  const Out obad = from_bits<Out>(g.bbad);
 #pragma unroll
-    for (int pv = 0; pv < OV; pv++) {
-      Out o[VO];
+  for (int q = 0; q < NV; q++) {
+    In x[VEC];
+    ldin(q, x);
+    Out o[VEC];
 #pragma unroll
-      for (int e = 0; e < VO; e++) {
-        const int j = pv * VO + e;
-        if (good(j)) {
-          run = S::add1(run, v[j]);
-          o[e] = S::value(run);
-        } else {
-          o[e] = obad;
-        }
+    for (int e = 0; e < VEC; e++) {
+      if (good(x[e])) {
+        run = S::add1(run, x[e]);
+        o[e] = S::value(run);
+      } else {
+        o[e] = obad;
       }
+    }
+#pragma unroll
+    for (int h = 0; h < VEC / VO; h++) {  // 1 (equal width) or 2 output vectors
+      const int pv = q * (VEC / VO) + h;
       float4 f;
-      memcpy(&f, o, 16);
-      const uint32_t dst = sb + (uint32_t)(lane * OV * 16 + ((pv ^ (lane & 7)) * 16));
+      memcpy(&f, &o[h * VO], 16);
+      const uint32_t dst = sout + (uint32_t)(lane * OV * 16 + ((pv ^ (lane & 7)) * 16));
       asm volatile("st.shared.v4.f32 [%0], {%1,%2,%3,%4};" ::"r"(dst), "f"(f.x), "f"(f.y),
                    "f"(f.z), "f"(f.w)
                    : "memory");
     }
-    __syncwarp();
+  }
+  __syncwarp();
+  Out *b = reinterpret_cast<Out *>(g.b) + offs[1];
+  if (fast) {
 #pragma unroll
     for (int r = 0; r < OV; r++) {
       const int gv = r * 32 + lane;
       const int own = gv / OV, pv = gv % OV;
-      const uint32_t src = sb + (uint32_t)(own * OV * 16 + ((pv ^ (own & 7)) * 16));
+      const uint32_t src = sout + (uint32_t)(own * OV * 16 + ((pv ^ (own & 7)) * 16));
       float4 f;
       asm volatile("ld.shared.v4.f32 {%0,%1,%2,%3}, [%4];"
                    : "=f"(f.x), "=f"(f.y), "=f"(f.z), "=f"(f.w)
@@ -463,17 +511,21 @@ __global__ void __launch_bounds__(CB, 4) k_scan_chain(const ScanArgs g, int64_t 
       __stcs(reinterpret_cast<float4 *>(b + wlo + (int64_t)gv * VO), f);
     }
   } else {
-    const int64_t t0 = wlo + (int64_t)lane * ITEMS;
-#pragma unroll
-    for (int j = 0; j < ITEMS; j++) {
-      if (j < nvalid) {
-        Out o = obad;
-        if (good(j)) {
-          run = S::add1(run, v[j]);
-          o = S::value(run);
-        }
-        b[t0 + j] = o;
+    for (int j = 0; j < nvalid; j++) {
+      const int pv = j / VO;
+      const uint32_t src = sout + (uint32_t)(lane * OV * 16 + ((pv ^ (lane & 7)) * 16)) +
+                           (uint32_t)((j % VO) * sizeof(Out));
+      Out o;
+      if constexpr (sizeof(Out) == 8) {
+        unsigned long long w;
+        asm volatile("ld.shared.u64 %0, [%1];" : "=l"(w) : "r"(src));
+        memcpy(&o, &w, 8);
+      } else {
+        unsigned int w;
+        asm volatile("ld.shared.u32 %0, [%1];" : "=r"(w) : "r"(src));
+        memcpy(&o, &w, 4);
       }
+      b[t0 + j] = o;
     }
   }
 }
@@ -513,7 +565,7 @@ pdlgb300_error scan_chain_typed(ScanArgs g, cudaStream_t s) {
   pdlgb300_error e = pgh::ok();
   if constexpr (chain_ok<In, Out>()) {
     constexpr int ITEMS = 128 / sizeof(In);
-    constexpr size_t smem = (size_t)CB * ITEMS * sizeof(Out);
+    constexpr size_t smem = (size_t)CB * 128 + (sizeof(Out) == sizeof(In) ? 0 : (size_t)CB * ITEMS * sizeof(Out));
     static bool attr = false;
     if (!attr) {
       cudaFuncSetAttribute(k_scan_chain<In, Out, 0, COMP>,
@@ -522,6 +574,12 @@ pdlgb300_error scan_chain_typed(ScanArgs g, cudaStream_t s) {
                            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       cudaFuncSetAttribute(k_scan_chain<In, Out, 2, COMP>,
                            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      cudaFuncSetAttribute(k_scan_chain<In, Out, 0, COMP>,
+                           cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+      cudaFuncSetAttribute(k_scan_chain<In, Out, 1, COMP>,
+                           cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+      cudaFuncSetAttribute(k_scan_chain<In, Out, 2, COMP>,
+                           cudaFuncAttributePreferredSharedMemoryCarveout, 100);
       attr = true;
     }
     const int64_t units = g.rows * g.nchunk;
