@@ -888,13 +888,22 @@ pdlgb300_error dispatch_reduce(RunCtx &c, int redop) {
     lc.grid = (int)std::min<int64_t>(units, (int64_t)1 << 30);
   }
   void *scratch = nullptr;
-  if (a.nsplit > 1) {
-    size_t accsz = red_acc_size(redop, c.v[0].datatype, a.f32_comp);
-    size_t need = (size_t)a.rows * a.nsplit * (accsz + sizeof(int64_t)) + 256;
+  // floating products (row kernel): per row, the first good exact zero
+  const int dtin = c.v[0].datatype;
+  const bool zfix = lc.kind == 0 && (redop == R_DPROD ||
+                                     (redop == R_PROD && (dtin == PDLGB300_F || dtin == PDLGB300_D)));
+  if (a.nsplit > 1 || zfix) {
+    size_t accsz = red_acc_size(redop, dtin, a.f32_comp);
+    size_t npart = a.nsplit > 1 ? (size_t)a.rows * a.nsplit : 0;
+    size_t off = (npart * accsz + 15) & ~(size_t)15;
+    size_t offz = off + ((npart * sizeof(int64_t) + 15) & ~(size_t)15);
+    size_t need = offz + (zfix ? (size_t)a.rows * sizeof(int64_t) : 0) + 256;
     RET_IF(dalloc(need, &scratch));
-    a.partials = scratch;
-    size_t off = ((size_t)a.rows * a.nsplit * accsz + 15) & ~(size_t)15;
-    a.pcounts = (int64_t *)((char *)scratch + off);
+    if (npart) {
+      a.partials = scratch;
+      a.pcounts = (int64_t *)((char *)scratch + off);
+    }
+    if (zfix) a.zidx = (int64_t *)((char *)scratch + offz);
   }
   pdlgb300_error e;
   const int dt = c.v[0].datatype;

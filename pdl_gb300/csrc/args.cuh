@@ -32,6 +32,7 @@ struct RedArgs {
   int nsplit;         // splits per row (1 = none)
   int group;          // threads per row (row kernel)
   int f32_comp;       // compensated float32 sums
+  int64_t *zidx;      // floating products: per row, first good exact zero (or INT64_MAX)
 };
 
 struct RedLaunch {

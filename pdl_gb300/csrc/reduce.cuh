@@ -82,6 +82,7 @@ template <class In, class Out, bool COMP> struct SumAcc {
 template <class In, class Out, bool COMP> struct OpSum {
   using S = SumAcc<In, Out, COMP>;
   using Acc = typename S::Acc;
+  static constexpr bool kZero = false, kLeftZero = false;
   static constexpr bool kCount = false, kVec = true, kNeutral = true;
   __device__ static In neutral() { return (In)0; }
   static constexpr bool kBlock = std::is_same_v<Acc, F64Sum>;
@@ -106,35 +107,67 @@ template <class In, class Out, bool COMP> struct OpSum {
   }
 };
 
+// Products.  The reference stops at the first element that makes the
+// running product zero (Ufunc.pd:107, `if (tmp == 0) break`).  Integer
+// products are unchanged by that (0 times anything wraps to 0); floating
+// ones would differ where inf or NaN follow a zero, so their accumulator
+// also carries the index of the first good exact zero, and rows that have
+// one are recomputed over [0, z] (k_prod_fix).  The sequential thread kernel
+// breaks exactly as the reference does.
+template <class Out> struct ProdZ {
+  Out p;
+  int64_t z;  // first good element equal to 0, or INT64_MAX
+};
 template <class In, class Out> struct OpProd {
-  using Acc = std::conditional_t<std::is_integral_v<Out>, uns_t<Out>, Out>;
+  static constexpr bool kZero = std::is_floating_point_v<Out>;
+  using Acc = std::conditional_t<std::is_integral_v<Out>, uns_t<Out>, ProdZ<Out>>;
   static constexpr bool kCount = false, kVec = true, kBlock = false, kNeutral = true;
+  static constexpr bool kLeftZero = true;
   __device__ static In neutral() { return (In)1; }
   static constexpr int kU = 0;
   template <int VEC, int U>
   __device__ static void add_block(Acc &, const In *, int64_t, int64_t) {}
-  __device__ static Acc init() { return (Acc)1; }
-  __device__ static void add(Acc &a, In v, int64_t) {
-    if constexpr (std::is_integral_v<Out>) a = (Acc)wmul<Out>((Out)a, (Out)v);
-    else a = rn_mul(a, (Out)v);
+  __device__ static Acc init() {
+    if constexpr (kZero) return Acc{(Out)1, INT64_MAX};
+    else return (Acc)1;
+  }
+  __device__ static void add(Acc &a, In v, int64_t i) {
+    if constexpr (kZero) {
+      const Out x = (Out)v;
+      a.p = rn_mul(a.p, x);
+      if (x == (Out)0 && i < a.z) a.z = i;
+    } else {
+      a = (Acc)wmul<Out>((Out)a, (Out)v);
+    }
   }
   template <int VEC> __device__ static void add_vec(Acc &a, const In *v, int64_t i) {
 #pragma unroll
     for (int e = 0; e < VEC; e++) add(a, v[e], i + e);
   }
   __device__ static void merge(Acc &a, const Acc &b) {
-    if constexpr (std::is_integral_v<Out>) a = (Acc)wmul<Out>((Out)a, (Out)b);
-    else a = rn_mul(a, b);
+    if constexpr (kZero) {
+      a.p = rn_mul(a.p, b.p);
+      if (b.z < a.z) a.z = b.z;
+    } else {
+      a = (Acc)wmul<Out>((Out)a, (Out)b);
+    }
+  }
+  // the running product is zero: the reference's loop stops here
+  __device__ static bool left_zero(const Acc &a) {
+    if constexpr (kZero) return a.p == (Out)0;
+    else return a == 0;
   }
   __device__ static Out fin(const Acc &a, int64_t cnt, bool bad, Out badval, int *) {
     if (bad && cnt == 0) return badval;
-    return (Out)a;
+    if constexpr (kZero) return a.p;
+    else return (Out)a;
   }
 };
 
 template <class In, class Out, bool COMP> struct OpAvg {
   using S = SumAcc<In, Out, COMP>;
   using Acc = typename S::Acc;
+  static constexpr bool kZero = false, kLeftZero = false;
   static constexpr bool kCount = true, kVec = true, kNeutral = true;
   __device__ static In neutral() { return (In)0; }
   static constexpr bool kBlock = std::is_same_v<Acc, F64Sum>;
@@ -180,6 +213,7 @@ template <class T> struct MMAcc {
 };
 template <class T, bool MAX, bool IND> struct OpMM {
   using Acc = MMAcc<T>;
+  static constexpr bool kZero = false, kLeftZero = false;
   using Out = std::conditional_t<IND, int64_t, T>;
   static constexpr bool kCount = false, kVec = true, kBlock = false, kNeutral = false;
   __device__ static T neutral() { return (T)0; }
@@ -231,6 +265,7 @@ __device__ __forceinline__ int64_t dkey(uint64_t b) {
 constexpr int64_t KEY_NAN = 0x7FFFFFFFFFFFFFFFll;
 
 template <bool MAX, bool IND> struct OpMM<double, MAX, IND> {
+  static constexpr bool kZero = false, kLeftZero = false;
   struct Acc {
     int64_t key;
     int64_t idx;  // -1: empty
@@ -517,6 +552,7 @@ __global__ void __launch_bounds__(512) k_red_rows(const RedArgs args) {
         int64_t cnt = (BAD || Op::kCount || args.inc_n != 1) ? ac.cnt : args.n;
         Out r = Op::fin(ac.acc, cnt, BAD, obad, args.setbad);
         store_out<Out>(args.b + offs[1] * (int64_t)sizeof(Out), r);
+        if constexpr (Op::kZero) args.zidx[row] = ac.acc.z;
       }
     }
   }
@@ -548,6 +584,47 @@ __global__ void k_red_combine(const RedArgs args) {
       const int64_t cnt = (BAD || Op::kCount || args.inc_n != 1) ? ac.cnt : args.n;
       Out r = Op::fin(ac.acc, cnt, BAD, obad, args.setbad);
       store_out<Out>(args.b + offs[1] * (int64_t)sizeof(Out), r);
+      if constexpr (Op::kZero) args.zidx[row] = ac.acc.z;
+    }
+  }
+}
+
+// Floating products of rows holding a good exact zero at z: the product of
+// elements [0, z], which is what the reference's loop leaves when it stops
+// at that zero (one warp per row; rows without a zero return at once).
+template <class Op, class In, class Out, bool BAD>
+__global__ void k_prod_fix(const RedArgs args) {
+  if constexpr (Op::kZero) {
+    using AC = AccCnt<typename Op::Acc>;
+    const int lane = threadIdx.x & 31;
+    const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
+    const Bad<In> bv{from_bits<In>(args.abad_bits), (bool)args.abad_isnan};
+    const Out obad = from_bits<Out>(args.bbad_bits);
+    for (int64_t row = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+         row < args.rows; row += nw) {
+      const int64_t z = args.zidx[row];
+      if (z >= args.n) continue;
+      int64_t offs[MAXP];
+      loop_offsets(args.L, row, offs);
+      const In *a = reinterpret_cast<const In *>(args.a) + offs[0];
+      AC ac{Op::init(), 0};
+      if (args.inc_n == 1) {
+        if constexpr (!BAD) {
+          row_accumulate<Op, In, 0>(a, 0, z + 1, lane, 32, bv.val, ac);
+        } else if constexpr (std::is_floating_point_v<In>) {
+          if (bv.isnan_) row_accumulate<Op, In, 2>(a, 0, z + 1, lane, 32, bv.val, ac);
+          else row_accumulate<Op, In, 1>(a, 0, z + 1, lane, 32, bv.val, ac);
+        } else {
+          row_accumulate<Op, In, 1>(a, 0, z + 1, lane, 32, bv.val, ac);
+        }
+      } else {
+        row_accumulate_strided<Op, In, BAD>(a, args.inc_n, 0, z + 1, lane, 32, bv, ac);
+      }
+      ac = group_reduce<Op>(ac, 32);
+      if (lane == 0) {
+        Out r = Op::fin(ac.acc, ac.cnt, BAD, obad, args.setbad);
+        store_out<Out>(args.b + offs[1] * (int64_t)sizeof(Out), r);
+      }
     }
   }
 }
@@ -570,6 +647,8 @@ __global__ void k_red_thread(const RedArgs args) {
       if (BAD && bv.is(v)) continue;
       Op::add(ac.acc, v, i);
       ac.cnt++;
+      if constexpr (Op::kLeftZero)
+        if (Op::left_zero(ac.acc)) break;
     }
     Out r = Op::fin(ac.acc, ac.cnt, BAD, obad, args.setbad);
     store_out<Out>(args.b + offs[1] * (int64_t)sizeof(Out), r);
@@ -579,29 +658,32 @@ __global__ void k_red_thread(const RedArgs args) {
 template <class Op, class In, class Out>
 pdlgb300_error launch_red_typed(RedArgs args, const RedLaunch &lc, cudaStream_t s) {
   pdlgb300_error e = pgh::ok();
-  const char *nm = "k_red";
+  auto launched = [&](const char *nm, int64_t grid, int block) {
+    if (!pgh::cuda_check(cudaGetLastError(), &e, nm)) return false;
+    pgh::record_kernel(nm, grid, block);
+    return true;
+  };
   if (lc.kind == 1) {
     if (args.bad) k_red_thread<Op, In, Out, true><<<lc.grid, lc.block, 0, s>>>(args);
     else k_red_thread<Op, In, Out, false><<<lc.grid, lc.block, 0, s>>>(args);
-    nm = "k_red_thread";
-  } else {
-    if (args.bad) k_red_rows<Op, In, Out, true><<<lc.grid, lc.block, 0, s>>>(args);
-    else k_red_rows<Op, In, Out, false><<<lc.grid, lc.block, 0, s>>>(args);
-    nm = "k_red_rows";
-    if (args.nsplit > 1) {
-      if (!pgh::cuda_check(cudaGetLastError(), &e, nm)) return e;
-      pgh::record_kernel(nm, lc.grid, lc.block);
-      int g = (int)std::min<int64_t>((args.rows + 3) / 4, 65535);
-      if (args.bad) k_red_combine<Op, In, Out, true><<<g, 128, 0, s>>>(args);
-      else k_red_combine<Op, In, Out, false><<<g, 128, 0, s>>>(args);
-      nm = "k_red_combine";
-      if (!pgh::cuda_check(cudaGetLastError(), &e, nm)) return e;
-      pgh::record_kernel(nm, g, 128);
-      return e;
-    }
+    launched("k_red_thread", lc.grid, lc.block);
+    return e;
   }
-  if (!pgh::cuda_check(cudaGetLastError(), &e, nm)) return e;
-  pgh::record_kernel(nm, lc.grid, lc.block);
+  if (args.bad) k_red_rows<Op, In, Out, true><<<lc.grid, lc.block, 0, s>>>(args);
+  else k_red_rows<Op, In, Out, false><<<lc.grid, lc.block, 0, s>>>(args);
+  if (!launched("k_red_rows", lc.grid, lc.block)) return e;
+  if (args.nsplit > 1) {
+    const int g = (int)std::min<int64_t>((args.rows + 3) / 4, 65535);
+    if (args.bad) k_red_combine<Op, In, Out, true><<<g, 128, 0, s>>>(args);
+    else k_red_combine<Op, In, Out, false><<<g, 128, 0, s>>>(args);
+    if (!launched("k_red_combine", g, 128)) return e;
+  }
+  if constexpr (Op::kZero) {
+    const int g = (int)std::min<int64_t>((args.rows + 7) / 8, 65535);
+    if (args.bad) k_prod_fix<Op, In, Out, true><<<g, 256, 0, s>>>(args);
+    else k_prod_fix<Op, In, Out, false><<<g, 256, 0, s>>>(args);
+    launched("k_prod_fix", g, 256);
+  }
   return e;
 }
 

@@ -390,3 +390,56 @@ def test_chained_scan_unaligned_rows_fall_back(gpu):
     got, exp = _run_both("cumusumover", [x])
     rtol, atol, scale = _tol("cumusumover", x.numpy(), exp, exp.type)
     assert_same(got, exp, rtol=rtol, atol=atol, scale=scale, what="cumusumover unaligned")
+
+
+@pytest.mark.parametrize("t", FLOAT_TYPES)
+@pytest.mark.parametrize("op", ["prodover", "dprodover"])
+def test_prodover_stops_at_first_zero(gpu, op, t):
+    """The reference's loop breaks once the running product is zero
+    (Ufunc.pd:107): inf or NaN after a zero leave it zero, a zero after an
+    inf gives NaN, and the zero's sign is the running product's at the
+    break.  Covers the row kernel, the split kernel and strided views."""
+    dt = NP_DTYPES[type_code(t)]
+    rows = np.array([[2, 0, np.nan, 5, 1],
+                     [3, -0.0, -1, -2, 1],
+                     [np.inf, 0, 1, 1, 1],
+                     [-1, 1, 0, np.inf, -7],
+                     [1, 2, 3, 4, 5],
+                     [0, 0, np.nan, 0, 1]], dtype=dt)
+    long = np.full((2, 300_000), 1.0, dtype=dt)
+    long[0, 100_000] = -0.0
+    long[0, 200_000] = np.nan
+    long[1, 250_000] = 0.0
+    long[1, 10] = -1.0
+    long[1, 299_999] = np.inf
+    for a in [rows, long, np.ascontiguousarray(rows.T)]:
+        x = to_pdl(a, t)
+        for v in [x, x.xchg(0, 1)] if a is not long else [x]:
+            got, exp = _run_both(op, [v])
+            g, e = got.numpy(), exp.numpy()
+            assert np.array_equal(np.isnan(g), np.isnan(e)), f"{op} {t}: NaN\n{g}\n{e}"
+            fin = ~np.isnan(e)
+            np.testing.assert_allclose(g[fin], e[fin], rtol=1e-6)
+            zero = fin & (e == 0)
+            assert np.array_equal(np.signbit(g[zero]), np.signbit(e[zero])), f"{op} {t}: sign of 0"
+
+
+def test_prodover_zero_in_bad_and_integer_rows(gpu):
+    rng = seeded(31)
+    a, bad = rand_array(rng, "double", (4, 5000), 0.9, 1.1, bad_frac=0.1)
+    a[1, 100] = 0.0
+    a[1, 101] = np.nan
+    a[2, 7] = 0.0
+    a[2, :7] = P.default_badvalue(type_code("double"))
+    x = to_pdl(a, "double", badflag=True)
+    got, exp = _run_both("prodover", [x])
+    assert np.array_equal(np.isnan(got.numpy()), np.isnan(exp.numpy()))
+    np.testing.assert_allclose(got.numpy(), exp.numpy(), rtol=1e-9)
+    ai, _ = rand_array(rng, "long", (3, 4000), -3, 3)
+    ai[0, 5] = 0
+    for op in ["prodover", "dprodover"]:
+        got, exp = _run_both(op, [to_pdl(ai, "long")])
+        if exp.type in FLOAT_TYPES:
+            np.testing.assert_allclose(got.numpy(), exp.numpy(), rtol=1e-9)
+        else:
+            assert_same(got, exp, what=f"{op} long")
