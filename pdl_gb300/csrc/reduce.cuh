@@ -217,7 +217,7 @@ template <class T, bool MAX, bool IND> struct OpMM {
   using Out = std::conditional_t<IND, int64_t, T>;
   static constexpr bool kCount = false, kVec = true, kBlock = false, kNeutral = false;
   __device__ static T neutral() { return (T)0; }
-  static constexpr int kU = 0;
+  static constexpr int kU = 8;
   template <int VEC, int U>
   __device__ static void add_block(Acc &, const T *, int64_t, int64_t) {}
   __device__ static Acc init() { return Acc{-1, (T)0}; }
@@ -416,7 +416,7 @@ __device__ __forceinline__ void row_accumulate(const In *row, int64_t lo, int64_
                                                int lane, int G, In bad,
                                                AccCnt<typename Op::Acc> &ac) {
   constexpr int VEC = 16 / sizeof(In);
-  constexpr int U = Op::kU ? Op::kU : 8;  // 16-byte vectors in flight per thread
+  constexpr int U = Op::kU ? Op::kU : 16;  // 16-byte vectors in flight per thread
   uint32_t nb = 0;
   auto take = [&](In v, int64_t idx, uint32_t &cnt) {
     if constexpr (BM == 0) {

@@ -226,7 +226,7 @@ __global__ void __launch_bounds__(256) k_scan_warp(const ScanArgs g) {
 // blocks were dispatched before it.  Every wait is bounded: on timeout the
 // status word gets bit 4 and the chunk goes on with what it has.
 constexpr int CB = 256;  // threads per chained-scan block
-constexpr int LB_PER_LANE = 4;  // look-back slots read per lane per round
+constexpr int LB_PER_LANE = 1;  // look-back slots read per lane per round
 
 __device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long *p) {
   unsigned long long v;
