@@ -863,8 +863,8 @@ pdlgb300_error dispatch_reduce(RunCtx &c, int redop) {
     lc.kind = 1;  // thread per row, coalesced across rows
     lc.block = 128;
     lc.grid = (int)std::min<int64_t>((a.rows + 127) / 128, (int64_t)nsm * 64);
-  } else if (a.n <= 1024) {
-    a.group = 32;
+  } else if (a.n * (int64_t)isz <= 32768) {
+    a.group = 32;  // rows up to 32 KiB: a warp per row, 8 rows per block
     lc.block = 256;
     lc.grid = (int)std::min<int64_t>((a.rows + 7) / 8, (int64_t)1 << 30);
   } else {

@@ -221,7 +221,7 @@ __global__ void __launch_bounds__(256) k_scan_warp(const ScanArgs g) {
 // Across the chunks of a row the carry travels by decoupled look-back:
 // each chunk publishes its total (A), then its inclusive prefix (P), in a
 // slot tagged with a 64-bit unit id (no reset between launches); a chunk
-// reads up to 128 predecessors per round and stops at the nearest P.
+// reads 32 predecessors per round (one per lane) and stops at the nearest P.
 // Chunks are taken in blockIdx order, so a chunk only waits on chunks whose
 // blocks were dispatched before it.  Every wait is bounded: on timeout the
 // status word gets bit 4 and the chunk goes on with what it has.
