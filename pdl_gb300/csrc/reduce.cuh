@@ -107,6 +107,12 @@ template <class In, class Out, bool COMP> struct OpSum {
   }
 };
 
+// x == 0 on the integer pipe (the float64 compare would use the FP64 pipe)
+template <class T> __device__ __forceinline__ bool is_zero_bits(T x) {
+  if constexpr (sizeof(T) == 8) return ((uint64_t)__double_as_longlong((double)x) << 1) == 0;
+  else return ((uint32_t)__float_as_uint((float)x) << 1) == 0;
+}
+
 // Products.  The reference stops at the first element that makes the
 // running product zero (Ufunc.pd:107, `if (tmp == 0) break`).  Integer
 // products are unchanged by that (0 times anything wraps to 0); floating
@@ -114,11 +120,6 @@ template <class In, class Out, bool COMP> struct OpSum {
 // also carries the index of the first good exact zero, and rows that have
 // one are recomputed over [0, z] (k_prod_fix).  The sequential thread kernel
 // breaks exactly as the reference does.
-// x == 0 on the integer pipe (the float64 compare would use the FP64 pipe)
-template <class T> __device__ __forceinline__ bool is_zero_bits(T x) {
-  if constexpr (sizeof(T) == 8) return ((uint64_t)__double_as_longlong((double)x) << 1) == 0;
-  else return ((uint32_t)__float_as_uint((float)x) << 1) == 0;
-}
 template <class Out> struct ProdZ {
   Out p;
   int64_t z;  // first good element equal to 0, or INT64_MAX
