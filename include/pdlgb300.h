@@ -247,6 +247,16 @@ pdlgb300_error pdlgb300_free(void *dptr);
  * its device mirror).  Synchronous. */
 pdlgb300_error pdlgb300_to_device(void *dptr, const void *host, size_t nbytes);
 pdlgb300_error pdlgb300_to_host(void *host, const void *dptr, size_t nbytes);
+/* The same transfers enqueued on `stream` (a cudaStream_t passed as a
+ * pointer; NULL: the library's stream) without waiting.  No counterpart in
+ * the reference, which has no device: a caller that pipelines copies
+ * against ops orders them with its own stream events, as with
+ * cudaMemcpyAsync; `host` must stay valid (and page-locked, for the copy to
+ * overlap anything) until that stream has passed the copy. */
+pdlgb300_error pdlgb300_to_device_async(void *dptr, const void *host, size_t nbytes,
+                                        void *stream);
+pdlgb300_error pdlgb300_to_host_async(void *host, const void *dptr, size_t nbytes,
+                                      void *stream);
 pdlgb300_error pdlgb300_sync(void);
 pdlgb300_error pdlgb300_device_count(int32_t *n);
 

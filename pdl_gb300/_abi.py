@@ -113,6 +113,8 @@ SIGNATURES = {
     "pdlgb300_free": (Error, [C.c_void_p]),
     "pdlgb300_to_device": (Error, [C.c_void_p, C.c_void_p, C.c_size_t]),
     "pdlgb300_to_host": (Error, [C.c_void_p, C.c_void_p, C.c_size_t]),
+    "pdlgb300_to_device_async": (Error, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]),
+    "pdlgb300_to_host_async": (Error, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]),
     "pdlgb300_sync": (Error, []),
     "pdlgb300_device_count": (Error, [C.POINTER(C.c_int32)]),
     "pdlgb300_last_launch": (Error, [C.POINTER(LaunchInfo)]),

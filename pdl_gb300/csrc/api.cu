@@ -1473,6 +1473,20 @@ pdlgb300_error pdlgb300_to_host(void *host, const void *dptr, size_t nbytes) {
   if (e != cudaSuccess) return err(PDLGB300_EFATAL, "to_host: %s", cudaGetErrorString(e));
   return ok();
 }
+pdlgb300_error pdlgb300_to_device_async(void *dptr, const void *host, size_t nbytes,
+                                        void *stream) {
+  cudaStream_t s = stream ? (cudaStream_t)stream : g_stream;
+  cudaError_t e = cudaMemcpyAsync(dptr, host, nbytes, cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return err(PDLGB300_EFATAL, "to_device_async: %s", cudaGetErrorString(e));
+  return ok();
+}
+pdlgb300_error pdlgb300_to_host_async(void *host, const void *dptr, size_t nbytes,
+                                      void *stream) {
+  cudaStream_t s = stream ? (cudaStream_t)stream : g_stream;
+  cudaError_t e = cudaMemcpyAsync(host, dptr, nbytes, cudaMemcpyDeviceToHost, s);
+  if (e != cudaSuccess) return err(PDLGB300_EFATAL, "to_host_async: %s", cudaGetErrorString(e));
+  return ok();
+}
 pdlgb300_error pdlgb300_sync(void) {
   cudaError_t e = cudaStreamSynchronize(g_stream);
   if (e != cudaSuccess) return err(PDLGB300_EFATAL, "sync: %s", cudaGetErrorString(e));

@@ -212,7 +212,7 @@ __global__ void __launch_bounds__(256) k_scan_warp(const ScanArgs g) {
 
 // ----------------------------------------------------------- chained scan
 // Contiguous, 16-byte aligned rows of 4- and 8-byte types: one block per
-// chunk of 32 KiB of input (8192 float32 / 4096 float64), each thread owning
+// chunk of a row (16384 elements of 4 bytes, 4096 of 8), each thread owning
 // 128 contiguous bytes.  Loads are striped 16-byte cp.async copies into a
 // shared-memory tile whose 16-byte slots are XOR-swizzled by lane, so both
 // the striped copies and each thread's blocked reads are free of bank
@@ -225,7 +225,11 @@ __global__ void __launch_bounds__(256) k_scan_warp(const ScanArgs g) {
 // Chunks are taken in blockIdx order, so a chunk only waits on chunks whose
 // blocks were dispatched before it.  Every wait is bounded: on timeout the
 // status word gets bit 4 and the chunk goes on with what it has.
-constexpr int CB = 256;  // threads per chained-scan block
+// threads per chained-scan block: 512 for 4-byte equal-width types (half
+// as many chunks to chain through look-back), 256 otherwise (shared memory)
+template <class In, class Out> constexpr int chain_threads() {
+  return (sizeof(In) == 4 && sizeof(Out) == 4) ? 512 : 256;
+}
 constexpr int LB_PER_LANE = 1;  // look-back slots read per lane per round
 
 __device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long *p) {
@@ -327,8 +331,9 @@ __device__ __forceinline__ Acc chain_lookback(const ScanArgs &g, ChainSlot *slot
 // look-back latency.  Equal-width outputs overwrite their input slots; wider
 // outputs (float32 -> float64) use a second, larger tile.
 template <class In, class Out, int BM, bool COMP>
-__global__ void __launch_bounds__(CB, sizeof(In) == 4 && sizeof(Out) == 4 ? 6 : 4)
+__global__ void __launch_bounds__(chain_threads<In, Out>(), (sizeof(In) == 4 && sizeof(Out) == 4) ? 3 : 4)
     k_scan_chain(const ScanArgs g, int64_t u0) {
+  constexpr int CB = chain_threads<In, Out>();
   using S = ScanT<In, Out, COMP>;
   using Acc = typename S::Acc;
   constexpr int ITEMS = 128 / sizeof(In);                // per thread
@@ -565,6 +570,7 @@ pdlgb300_error scan_chain_typed(ScanArgs g, cudaStream_t s) {
   pdlgb300_error e = pgh::ok();
   if constexpr (chain_ok<In, Out>()) {
     constexpr int ITEMS = 128 / sizeof(In);
+    constexpr int CB = chain_threads<In, Out>();
     constexpr size_t smem = (size_t)CB * 128 + (sizeof(Out) == sizeof(In) ? 0 : (size_t)CB * ITEMS * sizeof(Out));
     static bool attr = false;
     if (!attr) {
@@ -598,7 +604,7 @@ pdlgb300_error scan_chain_typed(ScanArgs g, cudaStream_t s) {
 }
 
 template <class In, class Out> constexpr int64_t chain_chunk() {
-  if constexpr (chain_ok<In, Out>()) return (int64_t)CB * (128 / sizeof(In));
+  if constexpr (chain_ok<In, Out>()) return (int64_t)chain_threads<In, Out>() * (128 / sizeof(In));
   return 0;
 }
 
