@@ -260,6 +260,9 @@ def run_ours(args, rank, world):
         result["f64_family"] = run_family(args, P, torch, stream, hbm)
     if args.matmult and rank == 0:
         result["matmult"] = bench_matmult(args, P, torch, stream, bf16, peak_kind)
+    if args.secondary and rank == 0:
+        result["fused_c2"] = bench_c2(args, P, torch, stream)
+        result["inner_c3"] = bench_inner(args, P, torch, stream, hbm)
     if rank == 0 and not args.no_cpu:
         result["cpu_baseline"] = cpu_baseline(args, mat)
     return result
@@ -474,6 +477,75 @@ def bench_matmult(args, P, torch, stream, bf16, peak_kind):
 
 # ------------------------------------------------------------- CPU baseline
 
+def time_op(torch, stream, fn, steps, warmup=3):
+    """Median device time (ms) of fn() on the library's stream."""
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    ts = []
+    for _ in range(steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ts.append(e0.elapsed_time(e1))
+    return statistics.median(ts)
+
+
+def bench_c2(args, P, torch, stream):
+    """Config 2: c = sumover(a*b + a), a (256,1,8192), b (256,512,1) ->
+    (512,8192), fused in one pass: int32 U{-1000..1000} (seed 2) and float32
+    N(0,1) with 2 % BAD in a and in b (seed 3)."""
+    out = {}
+    nops = 3 * 256 * 512 * 8192
+    nbytes = 4 * (256 * 8192 + 256 * 512 + 512 * 8192)
+    rng = np.random.default_rng(2)
+    a = rng.integers(-1000, 1001, size=(8192, 1, 256)).astype(np.int32)
+    b = rng.integers(-1000, 1001, size=(1, 512, 256)).astype(np.int32)
+    rng3 = np.random.default_rng(3)
+    af = rng3.standard_normal((8192, 1, 256)).astype(np.float32)
+    bf = rng3.standard_normal((1, 512, 256)).astype(np.float32)
+    bad = np.float32(-3.4028234663852886e38)
+    af[rng3.random(af.shape) < 0.02] = bad
+    bf[rng3.random(bf.shape) < 0.02] = bad
+    for name, (ha, hb, badflag) in {"int32": (a, b, False), "float32_bad": (af, bf, True)}.items():
+        x, y = P.pdl(ha), P.pdl(hb)
+        if badflag:
+            x.badflag(1)
+            y.badflag(1)
+        x.to_device()
+        y.to_device()
+        c = P.sumover_mult_plus(x, y, x)
+        P.sync()
+        kern = P.last_launch_info()["kernel"]
+        ms = time_op(torch, stream, lambda: P.sumover_mult_plus(x, y, x, c), args.mm_steps + 7)
+        out[name] = {"ms": ms, "gops": nops / (ms * 1e-3) / 1e9,
+                     "gbs": nbytes / (ms * 1e-3) / 1e9, "kernel": kern}
+    out["config"] = ("sumover(a*b+a): a (256,1,8192), b (256,512,1) -> (512,8192); "
+                     "int32 U{-1000..1000} seed 2; float32 N(0,1) seed 3 with 2% BAD")
+    out["bound"] = "int32 / fp32 pipe (3 ops per element evaluation, ~120 ops per byte)"
+    return out
+
+
+def bench_inner(args, P, torch, stream, hbm):
+    """Config 3 inner: float64 a, b dims (4096, 65536), U[-1,1) -> 65536."""
+    rng = np.random.default_rng(5)
+    a = rng.uniform(-1.0, 1.0, size=(65536, 4096))
+    b = rng.uniform(-1.0, 1.0, size=(65536, 4096))
+    x, y = P.pdl(a).to_device(), P.pdl(b).to_device()
+    del a, b
+    c = P.inner(x, y)
+    P.sync()
+    kern = P.last_launch_info()["kernel"]
+    ms = time_op(torch, stream, lambda: P.inner(x, y, c), args.mm_steps + 7)
+    nbytes = 2 * 4096 * 65536 * 8 + 65536 * 8
+    gbs = nbytes / (ms * 1e-3) / 1e9
+    return {"config": "inner, float64 a,b dims (4096,65536) U[-1,1) seed 5 -> 65536",
+            "ms": ms, "gbs": gbs, "frac_of_hbm": gbs / hbm, "kernel": kern,
+            "gflops": 2 * 4096 * 65536 / (ms * 1e-3) / 1e9}
+
+
 def cpu_time(mat, nrows, nthreads, budget_s, steps=None):
     """The oracle (the reference's loops in C, with its auto-pthread split)
     on `nrows` rows of the config-5 matrix; GB/s over the C5 ops."""
@@ -546,6 +618,8 @@ def main():
     ap.add_argument("--c5-ops", default=",".join(C5_OPS))
     ap.add_argument("--no-accuracy", dest="accuracy", action="store_false")
     ap.add_argument("--no-family", dest="family", action="store_false")
+    ap.add_argument("--no-secondary", dest="secondary", action="store_false",
+                    help="skip the fused sumover(a*b+a) and float64 inner timings")
     args = ap.parse_args()
     UFUNC_OPS = [o for o in args.ops.split(",") if o]
     rank = int(os.environ.get("RANK", 0))

@@ -657,6 +657,28 @@ pdlgb300_error setbad_word(int **out) {
   return ok();
 }
 
+// Per-row arrival counters of split reductions, per device: zeroed once;
+// every launch leaves them zero again (the last block of a row resets its
+// counter).
+constexpr int SPLIT_CTRS = 4096;
+int *g_split_ctr[64];
+pdlgb300_error split_counters(int **out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64)
+    return err(PDLGB300_EFATAL, "no current CUDA device");
+  std::lock_guard<std::mutex> lk(g_flag_mu);
+  if (!g_split_ctr[dev]) {
+    cudaError_t e = cudaMalloc((void **)&g_split_ctr[dev], SPLIT_CTRS * sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(g_split_ctr[dev], 0, SPLIT_CTRS * sizeof(int));
+    if (e != cudaSuccess) {
+      g_split_ctr[dev] = nullptr;
+      return err(PDLGB300_EFATAL, "device allocation failed: %s", cudaGetErrorString(e));
+    }
+  }
+  *out = g_split_ctr[dev];
+  return ok();
+}
+
 // Word 1 of the same allocation: set by kernels whose bounded waits gave up.
 pdlgb300_error status_word(int **out) {
   int *w = nullptr;
@@ -905,6 +927,9 @@ pdlgb300_error dispatch_reduce(RunCtx &c, int redop) {
     }
     if (zfix) a.zidx = (int64_t *)((char *)scratch + offz);
   }
+  // split rows: the last block of a row merges its partials (rows split
+  // only when there are fewer than 2 per SM, and a group is then a block)
+  if (a.nsplit > 1 && a.group == lc.block && a.rows <= SPLIT_CTRS) RET_IF(split_counters(&a.split_ctr));
   pdlgb300_error e;
   const int dt = c.v[0].datatype;
   if (redop == R_SUM || redop == R_DSUM || redop == R_AVG || redop == R_DAVG)

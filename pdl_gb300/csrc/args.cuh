@@ -33,6 +33,8 @@ struct RedArgs {
   int group;          // threads per row (row kernel)
   int f32_comp;       // compensated float32 sums
   int64_t *zidx;      // floating products: per row, first good exact zero (or INT64_MAX)
+  int *split_ctr;     // split mode: per-row arrival counters (zero between launches), or
+                      // nullptr for a separate combine kernel
 };
 
 struct RedLaunch {

@@ -506,6 +506,17 @@ __device__ __forceinline__ void row_accumulate_strided(const In *row, int64_t in
   }
 }
 
+// A value written by another block in this launch: read through L2.
+template <class T> __device__ __forceinline__ T ldcg_any(const T *p) {
+  static_assert(sizeof(T) % 4 == 0, "4-byte words");
+  unsigned w[sizeof(T) / 4];
+#pragma unroll
+  for (int i = 0; i < (int)(sizeof(T) / 4); i++) w[i] = __ldcg(reinterpret_cast<const unsigned *>(p) + i);
+  T v;
+  memcpy(&v, w, sizeof(T));
+  return v;
+}
+
 template <class Out> __device__ __forceinline__ void store_out(char *p, Out v) {
   *reinterpret_cast<Out *>(p) = v;
 }
@@ -551,15 +562,45 @@ __global__ void __launch_bounds__(512) k_red_rows(const RedArgs args) {
     } else
       row_accumulate_strided<Op, In, BAD>(a, args.inc_n, lo, hi, lane, G, bv, ac);
     ac = group_reduce<Op>(ac, G);
+    bool last = false;
     if (lane == 0) {
       if (args.nsplit > 1) {
         reinterpret_cast<Acc *>(args.partials)[u] = ac.acc;
         args.pcounts[u] = ac.cnt;
+        if (args.split_ctr) {
+          __threadfence();
+          last = atomicAdd(&args.split_ctr[row], 1) == args.nsplit - 1;
+        }
       } else {
         int64_t cnt = (BAD || Op::kCount || args.inc_n != 1) ? ac.cnt : args.n;
         Out r = Op::fin(ac.acc, cnt, BAD, obad, args.setbad);
         store_out<Out>(args.b + offs[1] * (int64_t)sizeof(Out), r);
         if constexpr (Op::kZero) args.zidx[row] = ac.acc.z;
+      }
+    }
+    if (args.nsplit > 1 && args.split_ctr) {
+      // the row's last split to arrive merges the row's partials (a group
+      // is the whole block whenever rows are split)
+      __shared__ int s_last;
+      if (lane == 0) s_last = last;
+      __syncthreads();
+      if (s_last) {
+        __threadfence();
+        const Acc *p = reinterpret_cast<const Acc *>(args.partials) + row * args.nsplit;
+        const int64_t *pc = args.pcounts + row * args.nsplit;
+        AC m{Op::init(), 0};
+        for (int sp = lane; sp < args.nsplit; sp += G) {
+          AC o{ldcg_any(p + sp), (int64_t)__ldcg((const long long *)(pc + sp))};
+          merge_ac<Op>(m, o);
+        }
+        m = group_reduce<Op>(m, G);
+        if (lane == 0) {
+          const int64_t cnt = (BAD || Op::kCount || args.inc_n != 1) ? m.cnt : args.n;
+          Out r = Op::fin(m.acc, cnt, BAD, obad, args.setbad);
+          store_out<Out>(args.b + offs[1] * (int64_t)sizeof(Out), r);
+          if constexpr (Op::kZero) args.zidx[row] = m.acc.z;
+          args.split_ctr[row] = 0;  // ready for the next launch
+        }
       }
     }
   }
@@ -679,7 +720,7 @@ pdlgb300_error launch_red_typed(RedArgs args, const RedLaunch &lc, cudaStream_t 
   if (args.bad) k_red_rows<Op, In, Out, true><<<lc.grid, lc.block, 0, s>>>(args);
   else k_red_rows<Op, In, Out, false><<<lc.grid, lc.block, 0, s>>>(args);
   if (!launched("k_red_rows", lc.grid, lc.block)) return e;
-  if (args.nsplit > 1) {
+  if (args.nsplit > 1 && !args.split_ctr) {
     const int g = (int)std::min<int64_t>((args.rows + 3) / 4, 65535);
     if (args.bad) k_red_combine<Op, In, Out, true><<<g, 128, 0, s>>>(args);
     else k_red_combine<Op, In, Out, false><<<g, 128, 0, s>>>(args);
