@@ -1111,7 +1111,7 @@ pdlgb300_error dispatch_inner(RunCtx &c) {
   tl_info.flops = 2.0 * g.rows * g.n;
   const bool contig = g.inc_a == 1 && g.inc_b == 1;
   if (!contig && g.rows >= 256LL * pgh::num_sms()) g.group = 0;
-  else g.group = g.n <= 1024 ? 32 : (g.n >= 16384 ? 256 : 128);
+  else g.group = g.n * (int64_t)TSIZES[c.v[0].datatype] <= 32768 ? 32 : (g.n >= 16384 ? 256 : 128);
   return launch_inner(c.ttype, g, g_stream);
 }
 

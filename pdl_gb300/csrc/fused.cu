@@ -129,16 +129,43 @@ __global__ void __launch_bounds__(FT) k_fused_outer(const FusedArgs g) {
 #pragma unroll
           for (int x = 0; x < 4; x++) FA::add(acc[y][x], wmul<T>(av[x], b1));
         }
+      } else if constexpr (BAD) {
+        // the inputs' bad tests once per staged value, not per pair; the
+        // intermediates' tests (t and u against their badvalue) per pair,
+        // with the NaN mode fixed per launch
+        const bool ft = g.fa || g.fb, fu = ft || g.fd;
+        bool xa[4], xd[4], xb[4];
+#pragma unroll
+        for (int x = 0; x < 4; x++) {
+          xa[x] = g.fa && ba.is(av[x]);
+          xd[x] = g.fd && bd.is(dv[x]);
+          xb[x] = g.fb && bb.is(bv[x]);
+        }
+        auto pairs = [&](auto tnan) {
+          constexpr bool TN = decltype(tnan)::value;
+          auto isbt = [&](T v) { return TN ? (v != v) : (v == tbad); };
+#pragma unroll
+          for (int y = 0; y < 4; y++)
+#pragma unroll
+            for (int x = 0; x < 4; x++) {
+              const T t = (xa[x] || xb[y]) ? tbad : op_mul<T>(av[x], bv[y]);
+              const T u = ((ft && isbt(t)) || xd[x]) ? ubad : op_add<T>(t, dv[x]);
+              if (!(fu && isbt(u))) {
+                FA::add(acc[y][x], u);
+                cnt[y][x]++;
+              }
+            }
+        };
+        if (bt.isnan_) pairs(std::true_type{});
+        else pairs(std::false_type{});
       } else {
 #pragma unroll
         for (int y = 0; y < 4; y++)
 #pragma unroll
           for (int x = 0; x < 4; x++) {
             T u;
-            if (chain<T, BAD>(g, av[x], bv[y], dv[x], ba, bb, bd, bt, tbad, ubad, u)) {
+            if (chain<T, BAD>(g, av[x], bv[y], dv[x], ba, bb, bd, bt, tbad, ubad, u))
               FA::add(acc[y][x], u);
-              if (BAD) cnt[y][x]++;
-            }
           }
       }
     }

@@ -61,7 +61,7 @@ __global__ void __launch_bounds__(256) k_inner_rows(const InnerArgs g) {
   using A = typename IA::A;
   using P = typename IA::P;
   constexpr int VEC = 16 / sizeof(T);
-  constexpr int U = sizeof(T) == 8 ? 8 : 4;
+  constexpr int U = 4;  // 16-byte vectors of each operand in flight (8 for float64 cost 174 registers)
   Bad<T> ba{from_bits<T>(g.abad), (bool)g.abad_isnan};
   Bad<T> bb{from_bits<T>(g.bbad), (bool)g.bbad_isnan};
   const T cbad = from_bits<T>(g.cbad);
