@@ -39,6 +39,10 @@ constexpr uint32_t B_TILE = TC_N * TC_BK * 2;  // 16 KiB
 constexpr uint32_t TMEM_COLS = 512;  // two 256-column slab accumulators
 constexpr long long WAIT_CYCLES = 8000000000LL;  // ~4 s at 2 GHz
 
+// K-slabs accumulated in one TMEM buffer before the accumulator warps
+// drain it into round-to-nearest registers
+constexpr int SPB = 1;
+
 template <int LIMBS> struct TcCfg {
   static constexpr int STAGES = LIMBS == 3 ? 3 : 4;
   static constexpr int NPROD = LIMBS == 3 ? 6 : 3;
@@ -197,14 +201,15 @@ __global__ void __launch_bounds__(320, 1)
       // ------------------------------------------------------------- MMA
       for (int kb = 0; kb < nk && ok; kb++) {
         const int s = kb % C::STAGES, use = kb / C::STAGES;
-        const int b = kb & 1, j = kb >> 1;
-        if (j > 0) ok = mbar_wait(&acce[b], (j - 1) & 1, g.err);
+        const int pr = kb / SPB, b = pr & 1, j = pr >> 1;
+        const bool opens = kb % SPB == 0, closes = kb % SPB == SPB - 1 || kb == nk - 1;
+        if (opens && j > 0) ok = mbar_wait(&acce[b], (j - 1) & 1, g.err);
         if (ok) ok = mbar_wait(&full[s], use & 1, g.err);
         if (!ok) break;
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         const uint32_t st = su32(base + s * C::STAGE_BYTES);
         const uint32_t d = tmem + (uint32_t)(b * TC_N);
-        int first = 1;
+        int first = opens ? 1 : 0;
 #pragma unroll
         for (int p = 0; p < C::NPROD; p++) {
 #pragma unroll
@@ -217,7 +222,7 @@ __global__ void __launch_bounds__(320, 1)
           }
         }
         umma_commit(&empty[s]);
-        umma_commit(&accf[b]);
+        if (closes) umma_commit(&accf[b]);
       }
     }
   } else {
@@ -229,9 +234,10 @@ __global__ void __launch_bounds__(320, 1)
 #pragma unroll
     for (int i = 0; i < 128; i++) acc[i] = 0.f;
     const uint32_t tl = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(half * 128);
-    for (int kb = 0; kb < nk && ok; kb++) {
-      const int b = kb & 1;
-      if (lane == 0) ok = mbar_wait(&accf[b], (kb >> 1) & 1, g.err);
+    const int npr = (nk + SPB - 1) / SPB;
+    for (int pr = 0; pr < npr && ok; pr++) {
+      const int b = pr & 1;
+      if (lane == 0) ok = mbar_wait(&accf[b], (pr >> 1) & 1, g.err);
       ok = __shfl_sync(0xffffffffu, ok, 0);  // warp-uniform for tcgen05.ld
       if (!ok) break;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
