@@ -54,7 +54,7 @@ FAMILY = "float64 dims (4096,2048) uniform[-1,1) seed 1, no bad values"
 # dram__bytes_read.sum + dram__bytes_write.sum per launch of the dominant
 # kernel on this workload, from the ncu captures summarised in profiles/
 # (captured at 1024 rows and scaled by 4 to the 4096-row matrix)
-NCU_TRAFFIC = {"cumusumover[matrix]": 4 * (268.763904e6 + 212.594688e6)}
+NCU_TRAFFIC = {"cumusumover[matrix]": 4 * (268.610304e6 + 207.915008e6)}
 
 
 def peaks():
@@ -530,20 +530,21 @@ def bench_c2(args, P, torch, stream):
 
 def bench_inner(args, P, torch, stream, hbm):
     """Config 3 inner: float64 a, b dims (4096, 65536), U[-1,1) -> 65536."""
+    cols = args.inner_cols
     rng = np.random.default_rng(5)
-    a = rng.uniform(-1.0, 1.0, size=(65536, 4096))
-    b = rng.uniform(-1.0, 1.0, size=(65536, 4096))
+    a = rng.uniform(-1.0, 1.0, size=(cols, 4096))
+    b = rng.uniform(-1.0, 1.0, size=(cols, 4096))
     x, y = P.pdl(a).to_device(), P.pdl(b).to_device()
     del a, b
     c = P.inner(x, y)
     P.sync()
     kern = P.last_launch_info()["kernel"]
     ms = time_op(torch, stream, lambda: P.inner(x, y, c), args.mm_steps + 7)
-    nbytes = 2 * 4096 * 65536 * 8 + 65536 * 8
+    nbytes = 2 * 4096 * cols * 8 + cols * 8
     gbs = nbytes / (ms * 1e-3) / 1e9
-    return {"config": "inner, float64 a,b dims (4096,65536) U[-1,1) seed 5 -> 65536",
+    return {"config": f"inner, float64 a,b dims (4096,{cols}) U[-1,1) seed 5 -> {cols}",
             "ms": ms, "gbs": gbs, "frac_of_hbm": gbs / hbm, "kernel": kern,
-            "gflops": 2 * 4096 * 65536 / (ms * 1e-3) / 1e9}
+            "gflops": 2 * 4096 * cols / (ms * 1e-3) / 1e9}
 
 
 def cpu_time(mat, nrows, nthreads, budget_s, steps=None):
@@ -620,6 +621,8 @@ def main():
     ap.add_argument("--no-family", dest="family", action="store_false")
     ap.add_argument("--no-secondary", dest="secondary", action="store_false",
                     help="skip the fused sumover(a*b+a) and float64 inner timings")
+    ap.add_argument("--inner-cols", type=int, default=65536,
+                    help="broadcast length of the float64 inner (smaller for profiling)")
     args = ap.parse_args()
     UFUNC_OPS = [o for o in args.ops.split(",") if o]
     rank = int(os.environ.get("RANK", 0))
