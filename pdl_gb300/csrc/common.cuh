@@ -7,6 +7,7 @@
 #include <cmath>
 #include <string>
 #include <type_traits>
+#include <utility>
 
 #include "../../include/pdlgb300.h"
 
@@ -84,10 +85,42 @@ template <class T> __host__ __device__ __forceinline__ T wmul(T a, T b) {
   }
 }
 
+// IEEE binary64 product, round to nearest even, on the integer pipe: GB300
+// multiplies doubles at a small fraction of its integer rate, which bounds
+// streaming float64 products below HBM speed.  Normal operands with a
+// normal (or overflowing) result take the 53 x 53-bit significand product
+// and round it here; zeros, subnormals, inf, NaN and results near the
+// underflow range go to the hardware multiply.  Same bits as __dmul_rn.
+__device__ __forceinline__ double dmul_rn_int(double a, double b) {
+  const uint64_t ua = (uint64_t)__double_as_longlong(a), ub = (uint64_t)__double_as_longlong(b);
+  const uint32_t ea = (uint32_t)(ua >> 52) & 0x7FFu, eb = (uint32_t)(ub >> 52) & 0x7FFu;
+  const int e = (int)(ea + eb) - 1023;  // exponent field when the significand product is < 2
+  if (ea - 1u >= 2046u || eb - 1u >= 2046u || e < 1 || e > 2045) return __dmul_rn(a, b);
+  constexpr uint64_t H = 1ull << 52;
+  const uint64_t ma = (ua & (H - 1)) | H, mb = (ub & (H - 1)) | H;
+  const uint64_t hi = __umul64hi(ma, mb), lo = ma * mb;  // product in [2^104, 2^106)
+  const bool top = (hi >> 41) != 0;                       // product >= 2^105
+  const uint64_t m = top ? ((hi << 11) | (lo >> 53)) : ((hi << 12) | (lo >> 52));
+  const uint64_t rem = lo & (top ? (2 * H - 1) : (H - 1));
+  const uint64_t half = top ? H : (H >> 1);
+  const uint64_t up = (rem > half || (rem == half && (m & 1))) ? 1u : 0u;
+  // m carries the hidden bit: (field - 1) << 52 plus m, and a rounding carry
+  // out of the significand moves into the exponent (to inf past the range)
+  const uint64_t mag = ((uint64_t)(e - 1 + (top ? 1 : 0)) << 52) + m + up;
+  return __longlong_as_double((long long)(((ua ^ ub) & (1ull << 63)) | mag));
+}
+
+// Products of a block spread over both pipes: even positions on the FP64
+// pipe, odd ones on the integer pipe (the same bits either way).
+template <int J> __device__ __forceinline__ double dmul_rn_split(double a, double b) {
+  if constexpr (J & 1) return dmul_rn_int(a, b);
+  else return __dmul_rn(a, b);
+}
+
 // Exact IEEE ops with no FMA contraction (PDL's C code rounds every
 // product and sum).
 __device__ __forceinline__ float rn_mul(float a, float b) { return __fmul_rn(a, b); }
-__device__ __forceinline__ double rn_mul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double rn_mul(double a, double b) { return dmul_rn_int(a, b); }
 __device__ __forceinline__ float rn_add(float a, float b) { return __fadd_rn(a, b); }
 __device__ __forceinline__ double rn_add(double a, double b) { return __dadd_rn(a, b); }
 template <class T> __device__ __forceinline__ T op_mul(T a, T b) {

@@ -55,6 +55,18 @@ template <class T> struct alignas(16) V16 {
   T e[16 / sizeof(T)];
 };
 
+// The products of a block; float64 ones alternate between the FP64 pipe and
+// the integer pipe (dmul_rn_split), which together keep up with HBM.
+template <class T, class IA, int U, int VEC, int... J>
+__device__ __forceinline__ void block_products(const V16<T> (&xa)[U], const V16<T> (&xb)[U],
+                                               typename IA::P *p,
+                                               std::integer_sequence<int, J...>) {
+  if constexpr (std::is_same_v<T, double>)
+    ((p[J] = dmul_rn_split<J>(xa[J / VEC].e[J % VEC], xb[J / VEC].e[J % VEC])), ...);
+  else
+    ((p[J] = IA::prod(xa[J / VEC].e[J % VEC], xb[J / VEC].e[J % VEC])), ...);
+}
+
 template <class T, bool BAD>
 __global__ void __launch_bounds__(256) k_inner_rows(const InnerArgs g) {
   using IA = InnerAcc<T>;
@@ -99,10 +111,7 @@ __global__ void __launch_bounds__(256) k_inner_rows(const InnerArgs g) {
       }
       if (full && !BAD) {
         P p[U * VEC];
-#pragma unroll
-        for (int u = 0; u < U; u++)
-#pragma unroll
-          for (int e = 0; e < VEC; e++) p[u * VEC + e] = IA::prod(xa[u].e[e], xb[u].e[e]);
+        block_products<T, IA, U, VEC>(xa, xb, p, std::make_integer_sequence<int, U * VEC>{});
         IA::template add_block<U * VEC>(acc, p);
       } else {
 #pragma unroll

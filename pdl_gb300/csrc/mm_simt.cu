@@ -19,6 +19,7 @@ template <class T, bool FUSED>
 __device__ __forceinline__ T mac(T acc, T a, T b) {
   if constexpr (std::is_floating_point_v<T>) {
     if constexpr (FUSED) return fma(a, b, acc);
+    else if constexpr (std::is_same_v<T, double>) return rn_add(acc, __dmul_rn(a, b));  // register-bound tile
     else return rn_add(acc, rn_mul(a, b));
   } else {
     return wadd<T>(acc, wmul<T>(a, b));

@@ -443,3 +443,34 @@ def test_prodover_zero_in_bad_and_integer_rows(gpu):
             np.testing.assert_allclose(got.numpy(), exp.numpy(), rtol=1e-9)
         else:
             assert_same(got, exp, what=f"{op} long")
+
+
+def test_float64_products_bit_exact_over_the_exponent_range(gpu):
+    """float64 products are formed on the integer pipe for normal operands
+    (hardware multiply for zeros, subnormals, inf, NaN and the underflow
+    range): bit-identical to IEEE round-to-nearest, through mult and through
+    inner with n=1 (whose output is the rounded product)."""
+    rng = np.random.default_rng(41)
+    n = 1 << 21
+    bits = rng.integers(0, 2 ** 63, size=(4, n), dtype=np.int64).astype(np.uint64)
+    bits[:, ::2] ^= np.uint64(1) << np.uint64(63)                      # both signs
+    bits[1] = (bits[1] & np.uint64(0x800FFFFFFFFFFFFF)) | (
+        rng.integers(1023 - 40, 1023 + 40, size=n).astype(np.uint64) << np.uint64(52))
+    bits[2] &= ~np.uint64(0xFFFFFFF)                                     # short significands: ties
+    bits[3] = (bits[3] & np.uint64(0x800FFFFFFFFFFFFF)) | (
+        rng.integers(0, 60, size=n).astype(np.uint64) << np.uint64(52))  # near underflow, subnormal
+    a = bits.view(np.float64).reshape(-1)
+    b = np.roll(a, 12345)
+    special = np.array([0.0, -0.0, np.inf, -np.inf, np.nan, 5e-324, -2.2250738585072014e-308,
+                        1.7976931348623157e308, 1.0, -1.0])
+    a = np.concatenate([a, np.repeat(special, len(special))])
+    b = np.concatenate([b, np.tile(special, len(special))])
+    with np.errstate(all="ignore"):
+        want = a * b
+    got = P.mult(P.pdl(a), P.pdl(b)).numpy()
+    same = (got.view(np.uint64) == want.view(np.uint64)) | (np.isnan(got) & np.isnan(want))
+    assert same.all(), f"{(~same).sum()} products differ, e.g. {a[~same][:3]} x {b[~same][:3]}"
+    got = P.inner(P.pdl(a.reshape(-1, 1)), P.pdl(b.reshape(-1, 1))).numpy().reshape(-1)
+    want = want + 0.0  # the reference's tmp = 0; tmp += a*b turns -0 into +0
+    same = (got.view(np.uint64) == want.view(np.uint64)) | (np.isnan(got) & np.isnan(want))
+    assert same.all(), f"inner n=1: {(~same).sum()} products differ"
