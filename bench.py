@@ -70,7 +70,7 @@ def c1_input():
     return rng.uniform(-1.0, 1.0, size=(N1, N0))  # numpy order: PDL dims (4096, 2048)
 
 
-def c5_inputs(rows=None):
+def c5_inputs(rows=None, long_row=True):
     """float32 (rows, n) matrix and one long row: lognormal(0, 4) magnitude,
     random sign, 1% set to float's default badvalue (-FLT_MAX)."""
     rows = rows or C5_ROWS
@@ -83,7 +83,8 @@ def c5_inputs(rows=None):
         v[rng.random(count, dtype=np.float32) < 0.01] = bad
         return v
 
-    return gen(C5_N * rows).reshape(rows, C5_N), gen(C5_LONG)
+    mat = gen(C5_N * rows).reshape(rows, C5_N)
+    return mat, (gen(C5_LONG) if long_row else None)
 
 
 def op_bytes(op, n=N0, rows=N1, isz=8, osz=8):
@@ -151,6 +152,14 @@ class Clocks:
                     reasons.add(n)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
                 "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def max_over_ranks(torch, value, device):
+    """The largest of every rank's value (each rank's device time): the job
+    is as slow as its slowest replica."""
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
 
 
 def timed_steps(torch, stream, steps, warmup, one_step, nops):
@@ -222,9 +231,7 @@ def run_ours(args, rank, world):
                                                   one_step, len(work))
     if world > 1:
         torch.distributed.barrier()
-        t = torch.tensor([total], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total = float(t.item())
+        total = max_over_ranks(torch, total, dev)
     step_bytes = sum(wbytes)
     ms_per_step = total / args.steps
     value = world * step_bytes / (ms_per_step * 1e-3) / 1e9
@@ -576,7 +583,7 @@ def cpu_baseline(args, mat):
 
 
 def run_reference(args, rank, world):
-    mat, _ = c5_inputs()
+    mat, _ = c5_inputs(args.c5_rows, long_row=False)
     n = os.cpu_count() or 1
     rows = 256
     cpu_time(mat, rows, n, 0.0, steps=max(1, args.warmup))
