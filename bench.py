@@ -471,7 +471,9 @@ def bench_matmult(args, P, torch, stream, bf16, peak_kind):
         err = 0.0
         for z in zs:
             ref = a[z][rows].astype(np.float64) @ b.astype(np.float64)
-            err = max(err, float(np.max(np.abs(cn[z][rows] - ref)) / np.max(np.abs(ref))))
+            diff = np.abs(cn[z][rows].astype(np.float64) - ref)
+            diff = np.where(np.isnan(diff), np.inf, diff)  # a NaN result is an error
+            err = max(err, float(np.max(diff) / np.max(np.abs(ref))))
         out[name] = {"tflops": flops / (ms * 1e-3) / 1e12, "ms": ms, "kernel": kern,
                      "max_normwise_rel_err": err}
     P.set_matmult_mode(P.MATMULT_BF16X6)
