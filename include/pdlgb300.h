@@ -163,6 +163,38 @@ pdlgb300_error pdlgb300_run_plus(pdlgb300_ndarray *a, pdlgb300_ndarray *b,
                                  pdlgb300_ndarray *c, int swap);
 pdlgb300_error pdlgb300_run_mult(pdlgb300_ndarray *a, pdlgb300_ndarray *b,
                                  pdlgb300_ndarray *c, int swap);
+/* The other binary ops of lib/PDL/Ops.pd:290-307, same convention as
+ * plus/mult (pdl_run_minus, pdl_run_divide, pdl_run_gt ... pdl_run_xor):
+ * c = a op b in the working type (comparisons give 0 or 1; shiftleft,
+ * shiftright, or2, and2, xor have the integer types as GenericTypes, so
+ * float inputs work in longlong).  Integer division by zero and shifts by a
+ * negative or too large count have no defined result in the reference's C. */
+pdlgb300_error pdlgb300_run_minus(pdlgb300_ndarray *a, pdlgb300_ndarray *b,
+                                  pdlgb300_ndarray *c, int swap);
+pdlgb300_error pdlgb300_run_divide(pdlgb300_ndarray *a, pdlgb300_ndarray *b,
+                                   pdlgb300_ndarray *c, int swap);
+pdlgb300_error pdlgb300_run_gt(pdlgb300_ndarray *a, pdlgb300_ndarray *b,
+                               pdlgb300_ndarray *c, int swap);
+pdlgb300_error pdlgb300_run_lt(pdlgb300_ndarray *a, pdlgb300_ndarray *b,
+                               pdlgb300_ndarray *c, int swap);
+pdlgb300_error pdlgb300_run_le(pdlgb300_ndarray *a, pdlgb300_ndarray *b,
+                               pdlgb300_ndarray *c, int swap);
+pdlgb300_error pdlgb300_run_ge(pdlgb300_ndarray *a, pdlgb300_ndarray *b,
+                               pdlgb300_ndarray *c, int swap);
+pdlgb300_error pdlgb300_run_eq(pdlgb300_ndarray *a, pdlgb300_ndarray *b,
+                               pdlgb300_ndarray *c, int swap);
+pdlgb300_error pdlgb300_run_ne(pdlgb300_ndarray *a, pdlgb300_ndarray *b,
+                               pdlgb300_ndarray *c, int swap);
+pdlgb300_error pdlgb300_run_shiftleft(pdlgb300_ndarray *a, pdlgb300_ndarray *b,
+                                      pdlgb300_ndarray *c, int swap);
+pdlgb300_error pdlgb300_run_shiftright(pdlgb300_ndarray *a, pdlgb300_ndarray *b,
+                                       pdlgb300_ndarray *c, int swap);
+pdlgb300_error pdlgb300_run_or2(pdlgb300_ndarray *a, pdlgb300_ndarray *b,
+                                pdlgb300_ndarray *c, int swap);
+pdlgb300_error pdlgb300_run_and2(pdlgb300_ndarray *a, pdlgb300_ndarray *b,
+                                 pdlgb300_ndarray *c, int swap);
+pdlgb300_error pdlgb300_run_xor(pdlgb300_ndarray *a, pdlgb300_ndarray *b,
+                                pdlgb300_ndarray *c, int swap);
 /* lib/PDL/Primitive.pd:48-76  inner: a(n); b(n); [o]c()                   */
 pdlgb300_error pdlgb300_run_inner(pdlgb300_ndarray *a, pdlgb300_ndarray *b,
                                   pdlgb300_ndarray *c);

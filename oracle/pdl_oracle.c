@@ -21,7 +21,8 @@
  *   - the per-element Code of each op, in the reference's sequential order:
  *     sumover/prodover (+d) lib/PDL/Ufunc.pd:94-118, cumusumover (+d)
  *     :120-140, average (+d) :413-444, minimum/maximum(+_ind) :446-500,
- *     plus/mult lib/PDL/Ops.pd:133-153, inner lib/PDL/Primitive.pd:48-76,
+ *     plus/mult and the other binary ops lib/PDL/Ops.pd:133-153,288-307,
+ *     inner lib/PDL/Primitive.pd:48-76,
  *     matmult lib/PDL/Primitive.pd:211-248 (same t-tile order);
  *   - badflag propagation to outputs lib/PDL/Core/pdlapi.c:760-808.
  *
@@ -110,8 +111,11 @@ enum {
   OP_SUMOVER, OP_DSUMOVER, OP_PRODOVER, OP_DPRODOVER, OP_CUMUSUMOVER,
   OP_DCUMUSUMOVER, OP_AVERAGE, OP_DAVERAGE, OP_MINIMUM, OP_MAXIMUM,
   OP_MINIMUM_IND, OP_MAXIMUM_IND, OP_PLUS, OP_MULT, OP_INNER, OP_MATMULT,
+  OP_MINUS, OP_DIVIDE, OP_GT, OP_LT, OP_LE, OP_GE, OP_EQ, OP_NE, OP_SHIFTLEFT,
+  OP_SHIFTRIGHT, OP_OR2, OP_AND2, OP_XOR,
   OP_N
 };
+#define IS_BIOP(op) ((op) == OP_PLUS || (op) == OP_MULT || ((op) >= OP_MINUS && (op) <= OP_XOR))
 
 #define TYPED 1  /* typed output */
 #define TPLUS 2  /* "int+" */
@@ -125,6 +129,7 @@ typedef struct {
   const char *ind_names[3];
   int out_typed;        /* 0, TYPED, TYPED|TPLUS for the output */
   int out_type;         /* typed output type */
+  int int_only;         /* GenericTypes = the integer types (bit ops) */
 } opdef;
 
 static const opdef OPS[OP_N] = {
@@ -145,6 +150,20 @@ static const opdef OPS[OP_N] = {
   {"inner", 3, 2, {"a", "b", "c"}, {1, 1, 0}, {{0}, {0}, {0}}, {"n"}, 0, -1},
   {"matmult", 3, 2, {"a", "b", "c"}, {2, 2, 2}, {{0, 1}, {2, 0}, {2, 1}},
    {"t", "h", "w"}, 0, -1},
+  /* lib/PDL/Ops.pd:290-307 */
+  {"minus", 3, 2, {"a", "b", "c"}, {0, 0, 0}, {{0}, {0}, {0}}, {0}, 0, -1},
+  {"divide", 3, 2, {"a", "b", "c"}, {0, 0, 0}, {{0}, {0}, {0}}, {0}, 0, -1},
+  {"gt", 3, 2, {"a", "b", "c"}, {0, 0, 0}, {{0}, {0}, {0}}, {0}, 0, -1},
+  {"lt", 3, 2, {"a", "b", "c"}, {0, 0, 0}, {{0}, {0}, {0}}, {0}, 0, -1},
+  {"le", 3, 2, {"a", "b", "c"}, {0, 0, 0}, {{0}, {0}, {0}}, {0}, 0, -1},
+  {"ge", 3, 2, {"a", "b", "c"}, {0, 0, 0}, {{0}, {0}, {0}}, {0}, 0, -1},
+  {"eq", 3, 2, {"a", "b", "c"}, {0, 0, 0}, {{0}, {0}, {0}}, {0}, 0, -1},
+  {"ne", 3, 2, {"a", "b", "c"}, {0, 0, 0}, {{0}, {0}, {0}}, {0}, 0, -1},
+  {"shiftleft", 3, 2, {"a", "b", "c"}, {0, 0, 0}, {{0}, {0}, {0}}, {0}, 0, -1, 1},
+  {"shiftright", 3, 2, {"a", "b", "c"}, {0, 0, 0}, {{0}, {0}, {0}}, {0}, 0, -1, 1},
+  {"or2", 3, 2, {"a", "b", "c"}, {0, 0, 0}, {{0}, {0}, {0}}, {0}, 0, -1, 1},
+  {"and2", 3, 2, {"a", "b", "c"}, {0, 0, 0}, {{0}, {0}, {0}}, {0}, 0, -1, 1},
+  {"xor", 3, 2, {"a", "b", "c"}, {0, 0, 0}, {{0}, {0}, {0}}, {0}, 0, -1, 1},
 };
 
 static int find_op(const char *name) {
@@ -247,21 +266,27 @@ static int param_error(errbuf *e, const opdef *op, int param,
 
 /* -------------------------------------------------------- type selection */
 
-/* pdl__transtype_select with GenericTypes = all real types (ldouble and the
- * complex types are not computed by this path). */
+/* pdl__transtype_select (lib/PDL/Core/pdlapi.c:1208-1235) with GenericTypes
+ * = all real types (ldouble and the complex types are not computed by this
+ * path), or the integer types for the bit ops: the largest allowed type
+ * among the untyped parameters, outputs first; a type above the last
+ * allowed one, or none, gives the last allowed type. */
 static int transtype_select(const opdef *op, pdlgb300_ndarray *const *pdls) {
-  int ret = -1;
+  const int last = op->int_only ? PDLGB300_LL : PDLGB300_D;
+  int ret = -1, use_last = 0;
   for (int i = op->npdls - 1; i >= 0; i--) {
     const pdlgb300_ndarray *p = pdls[i];
     int is_typed = (i >= op->nparents) && op->out_typed;
     if (!(p->state & PDLGB300_NOMYDIMS) && !is_typed) {
       int t = p->datatype;
-      if (t > PDLGB300_D) t = PDLGB300_D; /* not available: last gentype */
-      if (ret < t) ret = t;
+      int avail = t <= last;
+      if (!avail && t > last) use_last = 1;
+      if (avail && ret < t) ret = t;
     }
     if (i == op->nparents && ret != -1) return ret;
   }
-  return ret < 0 ? PDLGB300_D : ret;
+  if (use_last || ret < 0) ret = last;
+  return ret;
 }
 
 static int out_type_for(const opdef *op, int ttype) {
@@ -669,8 +694,44 @@ O_REAL_TYPES(DEF_MMS)
   }
 #define DEF_BIOPS(E, CT, SYM, IP, ISF, UNS) \
   DEF_BIOP(plus_##SYM, CT, SYM, ISF, +)     \
-  DEF_BIOP(mult_##SYM, CT, SYM, ISF, *)
+  DEF_BIOP(mult_##SYM, CT, SYM, ISF, *)     \
+  DEF_BIOP(minus_##SYM, CT, SYM, ISF, -)    \
+  DEF_BIOP(divide_##SYM, CT, SYM, ISF, /)   \
+  DEF_BIOP(gt_##SYM, CT, SYM, ISF, >)       \
+  DEF_BIOP(lt_##SYM, CT, SYM, ISF, <)       \
+  DEF_BIOP(le_##SYM, CT, SYM, ISF, <=)      \
+  DEF_BIOP(ge_##SYM, CT, SYM, ISF, >=)      \
+  DEF_BIOP(eq_##SYM, CT, SYM, ISF, ==)      \
+  DEF_BIOP(ne_##SYM, CT, SYM, ISF, !=)
 O_REAL_TYPES(DEF_BIOPS)
+/* shifts and bit ops: the integer types only (GenericTypes $T) */
+#define DEF_BITOPS(E, CT, SYM, IP, ISF, UNS) \
+  DEF_BIOP(shiftleft_##SYM, CT, SYM, 0, <<)  \
+  DEF_BIOP(shiftright_##SYM, CT, SYM, 0, >>) \
+  DEF_BIOP(or2_##SYM, CT, SYM, 0, |)         \
+  DEF_BIOP(and2_##SYM, CT, SYM, 0, &)        \
+  DEF_BIOP(xor_##SYM, CT, SYM, 0, ^)
+#define O_INT_TYPES(X)                        \
+  X(PDLGB300_SB, int8_t, A, int32_t, 0, 0)    \
+  X(PDLGB300_B, uint8_t, B, int32_t, 0, 1)    \
+  X(PDLGB300_S, int16_t, S, int32_t, 0, 0)    \
+  X(PDLGB300_US, uint16_t, U, int32_t, 0, 1)  \
+  X(PDLGB300_L, int32_t, L, int32_t, 0, 0)    \
+  X(PDLGB300_UL, uint32_t, K, uint32_t, 0, 1) \
+  X(PDLGB300_IND, int64_t, N, int64_t, 0, 0)  \
+  X(PDLGB300_ULL, uint64_t, P, uint64_t, 0, 1)\
+  X(PDLGB300_LL, int64_t, Q, int64_t, 0, 0)
+O_INT_TYPES(DEF_BITOPS)
+#define shiftleft_F NULL
+#define shiftleft_D NULL
+#define shiftright_F NULL
+#define shiftright_D NULL
+#define or2_F NULL
+#define or2_D NULL
+#define and2_F NULL
+#define and2_D NULL
+#define xor_F NULL
+#define xor_D NULL
 
 /* inner: long double accumulator, product in the generic type */
 #define DEF_INNER(NAME, T, SYM, ISF)                                                    \
@@ -782,6 +843,19 @@ static body_fn pick_body(int op, int t) {
     CASE(OP_MULT, mult)
     CASE(OP_INNER, inner)
     CASE(OP_MATMULT, matmult)
+    CASE(OP_MINUS, minus)
+    CASE(OP_DIVIDE, divide)
+    CASE(OP_GT, gt)
+    CASE(OP_LT, lt)
+    CASE(OP_LE, le)
+    CASE(OP_GE, ge)
+    CASE(OP_EQ, eq)
+    CASE(OP_NE, ne)
+    CASE(OP_SHIFTLEFT, shiftleft)
+    CASE(OP_SHIFTRIGHT, shiftright)
+    CASE(OP_OR2, or2)
+    CASE(OP_AND2, and2)
+    CASE(OP_XOR, xor)
   }
 #undef CASE
   return NULL;
@@ -900,7 +974,7 @@ int oracle_run(const char *opname, pdlgb300_ndarray **pdls_in, const int64_t *ot
     local[j] = *pdls_in[j];
     pdls[j] = &local[j];
   }
-  if ((op == OP_PLUS || op == OP_MULT) && other && other[0]) {
+  if (IS_BIOP(op) && other && other[0]) {
     pdlgb300_ndarray t = local[0];
     local[0] = local[1];
     local[1] = t;

@@ -97,6 +97,9 @@ SIGNATURES = {
     "pdlgb300_run_maximum_ind": (Error, [P, P]),
     "pdlgb300_run_plus": (Error, [P, P, P, C.c_int]),
     "pdlgb300_run_mult": (Error, [P, P, P, C.c_int]),
+    **{f"pdlgb300_run_{op}": (Error, [P, P, P, C.c_int])
+       for op in ("minus", "divide", "gt", "lt", "le", "ge", "eq", "ne", "shiftleft",
+                  "shiftright", "or2", "and2", "xor")},
     "pdlgb300_run_inner": (Error, [P, P, P]),
     "pdlgb300_run_matmult": (Error, [P, P, P]),
     "pdlgb300_run_sumover_mult_plus": (Error, [P, P, P, P]),

@@ -114,13 +114,28 @@ namespace {
 enum OpId {
   O_SUMOVER, O_DSUMOVER, O_PRODOVER, O_DPRODOVER, O_CUMUSUMOVER, O_DCUMUSUMOVER,
   O_AVERAGE, O_DAVERAGE, O_MINIMUM, O_MAXIMUM, O_MINIMUM_IND, O_MAXIMUM_IND,
-  O_PLUS, O_MULT, O_INNER, O_MATMULT, O_SMP, O_NOPS
+  O_PLUS, O_MULT, O_INNER, O_MATMULT, O_SMP,
+  O_MINUS, O_DIVIDE, O_GT, O_LT, O_LE, O_GE, O_EQ, O_NE,
+  O_SHIFTLEFT, O_SHIFTRIGHT, O_OR2, O_AND2, O_XOR, O_NOPS
 };
+
+// binary ops (a(); b(); [o]c(); int swap) and their kernel codes
+bool is_biop(int op) { return op == O_PLUS || op == O_MULT || (op >= O_MINUS && op <= O_XOR); }
+int biop_code_of(int op) {
+  switch (op) {
+    case O_PLUS: return 0;
+    case O_MULT: return 1;
+    default: return 2 + (op - O_MINUS);  // minus, divide, gt .. xor in kernel order
+  }
+}
 
 const int32_t GENTYPES[] = {PDLGB300_SB, PDLGB300_B,   PDLGB300_S,   PDLGB300_US,
                             PDLGB300_L,  PDLGB300_UL,  PDLGB300_IND, PDLGB300_ULL,
                             PDLGB300_LL, PDLGB300_F,   PDLGB300_D,   PDLGB300_LD,
                             PDLGB300_CF, PDLGB300_CD,  PDLGB300_CLD, -1};
+// GenericTypes of the bit ops: the integer types (lib/PDL/Ops.pd:296-307)
+const int32_t INTTYPES[] = {PDLGB300_SB, PDLGB300_B,   PDLGB300_S,   PDLGB300_US, PDLGB300_L,
+                            PDLGB300_UL, PDLGB300_IND, PDLGB300_ULL, PDLGB300_LL, -1};
 const int32_t REALTYPES[] = {PDLGB300_SB, PDLGB300_B,  PDLGB300_S,   PDLGB300_US,
                              PDLGB300_L,  PDLGB300_UL, PDLGB300_IND, PDLGB300_ULL,
                              PDLGB300_LL, PDLGB300_F,  PDLGB300_D,   PDLGB300_LD, -1};
@@ -164,6 +179,19 @@ const pdlgb300_vtable VT[O_NOPS] = {
     {"inner", 3, 2, 1, 0, N_ABC, RD_110, F_ABC, PT_NONE, ID_NN, I_N, GENTYPES},
     {"matmult", 3, 2, 3, 0, N_ABC, RD_222, F_ABC, PT_NONE, ID_MM, I_THW, GENTYPES},
     {"sumover_mult_plus", 4, 3, 1, 0, N_ABDC, RD_1110, F_SMP, PT_SMP, ID_NNN, I_N, GENTYPES},
+    {"minus", 3, 2, 0, 1, N_ABC, RD_000, F_ABC, PT_NONE, ID_NONE, nullptr, GENTYPES},
+    {"divide", 3, 2, 0, 1, N_ABC, RD_000, F_ABC, PT_NONE, ID_NONE, nullptr, GENTYPES},
+    {"gt", 3, 2, 0, 1, N_ABC, RD_000, F_ABC, PT_NONE, ID_NONE, nullptr, GENTYPES},
+    {"lt", 3, 2, 0, 1, N_ABC, RD_000, F_ABC, PT_NONE, ID_NONE, nullptr, GENTYPES},
+    {"le", 3, 2, 0, 1, N_ABC, RD_000, F_ABC, PT_NONE, ID_NONE, nullptr, GENTYPES},
+    {"ge", 3, 2, 0, 1, N_ABC, RD_000, F_ABC, PT_NONE, ID_NONE, nullptr, GENTYPES},
+    {"eq", 3, 2, 0, 1, N_ABC, RD_000, F_ABC, PT_NONE, ID_NONE, nullptr, GENTYPES},
+    {"ne", 3, 2, 0, 1, N_ABC, RD_000, F_ABC, PT_NONE, ID_NONE, nullptr, GENTYPES},
+    {"shiftleft", 3, 2, 0, 1, N_ABC, RD_000, F_ABC, PT_NONE, ID_NONE, nullptr, INTTYPES},
+    {"shiftright", 3, 2, 0, 1, N_ABC, RD_000, F_ABC, PT_NONE, ID_NONE, nullptr, INTTYPES},
+    {"or2", 3, 2, 0, 1, N_ABC, RD_000, F_ABC, PT_NONE, ID_NONE, nullptr, INTTYPES},
+    {"and2", 3, 2, 0, 1, N_ABC, RD_000, F_ABC, PT_NONE, ID_NONE, nullptr, INTTYPES},
+    {"xor", 3, 2, 0, 1, N_ABC, RD_000, F_ABC, PT_NONE, ID_NONE, nullptr, INTTYPES},
 };
 
 int op_of(const pdlgb300_vtable *vt) {
@@ -564,15 +592,32 @@ int bad_isnan(const pdlgb300_ndarray *x) {
 // Type selection, pdl__transtype_select: the highest type among the
 // outputs that were supplied, else among the inputs; typed outputs (int+,
 // double, indx) do not vote.
+// pdl__transtype_select (lib/PDL/Core/pdlapi.c:1208-1235): the largest
+// type among the untyped parameters that GenericTypes allows, outputs
+// voting first; a type above the last allowed one (or none at all) gives
+// the last allowed type.
 int transtype_select(const pdlgb300_vtable *vt, pdlgb300_ndarray *const *pdls) {
+  bool avail[PDLGB300_NTYPES] = {false};
+  int last = -1, ngen = 0;
+  for (int k = 0; vt->gentypes[k] >= 0; k++, ngen++) {
+    avail[vt->gentypes[k]] = true;
+    last = vt->gentypes[k];
+  }
+  if (ngen == 1) return last;
   int ret = -1;
+  bool use_last = false;
   for (int i = vt->npdls - 1; i >= 0; i--) {
     const pdlgb300_ndarray *p = pdls[i];
-    if (!(p->state & PDLGB300_NOMYDIMS) && !(vt->par_flags[i] & PDLGB300_PARAM_ISTYPED))
-      ret = std::max(ret, (int)p->datatype);
+    if (!(p->state & PDLGB300_NOMYDIMS) && !(vt->par_flags[i] & PDLGB300_PARAM_ISTYPED)) {
+      const int t = p->datatype;
+      const bool ok = t >= 0 && t < PDLGB300_NTYPES && avail[t];
+      if (!ok && t > last) use_last = true;
+      if (ok && ret < t) ret = t;
+    }
     if (i == vt->nparents && ret != -1) return ret;
   }
-  return ret < 0 ? PDLGB300_D : ret;
+  if (use_last || ret < 0 || !avail[ret]) ret = last;
+  return ret;
 }
 
 int out_type(const pdlgb300_vtable *vt, int i, int ttype) {
@@ -704,7 +749,7 @@ pdlgb300_error run_impl(const pdlgb300_vtable *vt, pdlgb300_ndarray *const *pdls
     if (!pdls_in[i]) return err(PDLGB300_EUSERERROR, "%s: parameter %d is NULL", vt->name, i);
     c.user[i] = pdls_in[i];
   }
-  if ((op == O_PLUS || op == O_MULT) && other && other[0]) std::swap(c.user[0], c.user[1]);
+  if (is_biop(op) && other && other[0]) std::swap(c.user[0], c.user[1]);
   for (int i = 0; i < np; i++) {
     const pdlgb300_ndarray *p = c.user[i];
     if (p->state & PDLGB300_NOMYDIMS) continue;
@@ -785,7 +830,7 @@ pdlgb300_error run_impl(const pdlgb300_vtable *vt, pdlgb300_ndarray *const *pdls
   const bool minmax = op == O_MINIMUM || op == O_MAXIMUM || op == O_MINIMUM_IND ||
                       op == O_MAXIMUM_IND;
   const bool need_flag = (minmax && (c.bvalflag || c.b.ind_sizes[0] == 0)) ||
-                         ((op == O_PLUS || op == O_MULT || op == O_INNER) && c.bvalflag);
+                         ((is_biop(op) || op == O_INNER) && c.bvalflag);
   if (!e.error) e = setbad_word(&c.d_setbad);
   if (!e.error && need_flag) {
     cudaError_t ce = cudaMemsetAsync(c.d_setbad, 0, sizeof(int), g_stream);
@@ -1232,8 +1277,10 @@ pdlgb300_error dispatch(RunCtx &c, const int64_t *) {
     case O_MAXIMUM_IND: return dispatch_reduce(c, R_MAX_IND);
     case O_CUMUSUMOVER: return dispatch_cumusum(c, 0);
     case O_DCUMUSUMOVER: return dispatch_cumusum(c, 1);
-    case O_PLUS: return dispatch_biop(c, 0);
-    case O_MULT: return dispatch_biop(c, 1);
+    case O_PLUS: case O_MULT: case O_MINUS: case O_DIVIDE: case O_GT: case O_LT: case O_LE:
+    case O_GE: case O_EQ: case O_NE: case O_SHIFTLEFT: case O_SHIFTRIGHT: case O_OR2:
+    case O_AND2: case O_XOR:
+      return dispatch_biop(c, biop_code_of(c.op));
     case O_INNER: return dispatch_inner(c);
     case O_MATMULT: return dispatch_matmult(c);
     case O_SMP: return dispatch_smp(c);
@@ -1324,7 +1371,7 @@ pdlgb300_error pdlgb300_redodims(const pdlgb300_vtable *vt, pdlgb300_ndarray *co
     if (!pdls[i]) return err(PDLGB300_EUSERERROR, "%s: parameter %d is NULL", vt->name, i);
     p[i] = pdls[i];
   }
-  if ((op == O_PLUS || op == O_MULT) && other && other[0]) std::swap(p[0], p[1]);
+  if (is_biop(op) && other && other[0]) std::swap(p[0], p[1]);
   int tt = transtype_select(vt, p);
   Brc b;
   RET_IF(plan_broadcast(vt, p, b));
@@ -1373,6 +1420,28 @@ pdlgb300_error pdlgb300_run_mult(pdlgb300_ndarray *a, pdlgb300_ndarray *b, pdlgb
   int64_t o = swap;
   return guard_run(O_MULT, p, &o);
 }
+#define RUNBI(NAME, OP)                                                                   \
+  pdlgb300_error pdlgb300_run_##NAME(pdlgb300_ndarray *a, pdlgb300_ndarray *b,             \
+                                     pdlgb300_ndarray *c, int swap) {                      \
+    pdlgb300_ndarray *p[3] = {a, b, c};                                                    \
+    int64_t o = swap;                                                                      \
+    return guard_run(OP, p, &o);                                                           \
+  }
+RUNBI(minus, O_MINUS)
+RUNBI(divide, O_DIVIDE)
+RUNBI(gt, O_GT)
+RUNBI(lt, O_LT)
+RUNBI(le, O_LE)
+RUNBI(ge, O_GE)
+RUNBI(eq, O_EQ)
+RUNBI(ne, O_NE)
+RUNBI(shiftleft, O_SHIFTLEFT)
+RUNBI(shiftright, O_SHIFTRIGHT)
+RUNBI(or2, O_OR2)
+RUNBI(and2, O_AND2)
+RUNBI(xor, O_XOR)
+#undef RUNBI
+
 pdlgb300_error pdlgb300_run_inner(pdlgb300_ndarray *a, pdlgb300_ndarray *b,
                                   pdlgb300_ndarray *c) {
   pdlgb300_ndarray *p[3] = {a, b, c};

@@ -1,5 +1,6 @@
-// elem.cu -- PDL::Ops plus/mult under broadcasting (lib/PDL/Ops.pd:104-153,
-// 288-289) and type conversion (lib/PDL/Core/pdlconv.c:163-172).
+// elem.cu -- PDL::Ops binary ops under broadcasting (lib/PDL/Ops.pd:104-153,
+// 288-307: plus, mult, minus, divide, the comparisons, shifts and bit ops)
+// and type conversion (lib/PDL/Core/pdlconv.c:163-172).
 //
 // One thread per output element along the innermost collapsed broadcast dim
 // (coalesced), the outer dims flattened onto grid.y.  A fully contiguous
@@ -9,9 +10,48 @@
 
 namespace pg {
 
+// Binary op codes (lib/PDL/Ops.pd:288-307): each computes `$c() = $a() op
+// $b()` in the working type T, as the reference's C does: integers wrap,
+// floats are IEEE-rounded with no contraction, comparisons give 0 or 1,
+// shifts and bit ops exist for integer types only.
+enum BiopCode {
+  B_PLUS, B_MULT, B_MINUS, B_DIVIDE, B_GT, B_LT, B_LE, B_GE, B_EQ, B_NE,
+  B_SHL, B_SHR, B_OR2, B_AND2, B_XOR, B_NCODES
+};
+
+template <int OP> constexpr bool biop_int_only() {
+  return OP == B_SHL || OP == B_SHR || OP == B_OR2 || OP == B_AND2 || OP == B_XOR;
+}
+
 template <class T, int OP>
 __device__ __forceinline__ T biop_apply(T a, T b) {
-  return OP == 0 ? op_add<T>(a, b) : op_mul<T>(a, b);
+  if constexpr (OP == B_PLUS) return op_add<T>(a, b);
+  else if constexpr (OP == B_MULT) return op_mul<T>(a, b);
+  else if constexpr (OP == B_MINUS) {
+    if constexpr (std::is_floating_point_v<T>) return std::is_same_v<T, float> ? (T)__fsub_rn(a, b) : (T)__dsub_rn(a, b);
+    else return (T)(uns_t<T>)((uns_t<T>)a - (uns_t<T>)b);
+  } else if constexpr (OP == B_DIVIDE) {
+    // integer division by zero (and the minimum over -1) has no defined
+    // result in the reference's C; the GPU gives its own value there
+    if constexpr (std::is_same_v<T, float>) return __fdiv_rn(a, b);
+    else if constexpr (std::is_same_v<T, double>) return __ddiv_rn(a, b);
+    else return (T)(a / b);
+  } else if constexpr (OP == B_GT) return (T)(a > b);
+  else if constexpr (OP == B_LT) return (T)(a < b);
+  else if constexpr (OP == B_LE) return (T)(a <= b);
+  else if constexpr (OP == B_GE) return (T)(a >= b);
+  else if constexpr (OP == B_EQ) return (T)(a == b);
+  else if constexpr (OP == B_NE) return (T)(a != b);
+  else if constexpr (std::is_integral_v<T>) {
+    // C's usual promotions, then back to T
+    if constexpr (OP == B_SHL) return (T)(a << b);
+    else if constexpr (OP == B_SHR) return (T)(a >> b);
+    else if constexpr (OP == B_OR2) return (T)(a | b);
+    else if constexpr (OP == B_AND2) return (T)(a & b);
+    else return (T)(a ^ b);
+  } else {
+    return a;  // not instantiated: type selection gives bit ops an integer type
+  }
 }
 
 template <class T, int OP, bool BAD>
@@ -117,12 +157,35 @@ static pdlgb300_error biop_typed(const BiopArgs &g, cudaStream_t s) {
   return e;
 }
 
+template <class T, int OP>
+static pdlgb300_error biop_code(const BiopArgs &g, cudaStream_t s) {
+  if constexpr (biop_int_only<OP>() && !std::is_integral_v<T>)
+    return pgh::err(PDLGB300_EUSERERROR, "bit operations need an integer type");
+  else return biop_typed<T, OP>(g, s);
+}
+
 pdlgb300_error launch_biop(int op, int dt, const BiopArgs &g, cudaStream_t s) {
   PG_DISPATCH(dt, {
     using T = typename TT<DT>::T;
-    return op == 0 ? biop_typed<T, 0>(g, s) : biop_typed<T, 1>(g, s);
+    switch (op) {
+      case B_PLUS: return biop_code<T, B_PLUS>(g, s);
+      case B_MULT: return biop_code<T, B_MULT>(g, s);
+      case B_MINUS: return biop_code<T, B_MINUS>(g, s);
+      case B_DIVIDE: return biop_code<T, B_DIVIDE>(g, s);
+      case B_GT: return biop_code<T, B_GT>(g, s);
+      case B_LT: return biop_code<T, B_LT>(g, s);
+      case B_LE: return biop_code<T, B_LE>(g, s);
+      case B_GE: return biop_code<T, B_GE>(g, s);
+      case B_EQ: return biop_code<T, B_EQ>(g, s);
+      case B_NE: return biop_code<T, B_NE>(g, s);
+      case B_SHL: return biop_code<T, B_SHL>(g, s);
+      case B_SHR: return biop_code<T, B_SHR>(g, s);
+      case B_OR2: return biop_code<T, B_OR2>(g, s);
+      case B_AND2: return biop_code<T, B_AND2>(g, s);
+      case B_XOR: return biop_code<T, B_XOR>(g, s);
+    }
   });
-  return pgh::err(PDLGB300_EUSERERROR, "plus/mult: unsupported type %d", dt);
+  return pgh::err(PDLGB300_EUSERERROR, "binary op: unsupported type %d or op %d", dt, op);
 }
 
 // ------------------------------------------------------------ conversion

@@ -253,6 +253,20 @@ class ndarray:
     def __matmul__(self, o):
         return matmult(self, o)
 
+    def __sub__(self, o): return minus(self, o)
+    def __rsub__(self, o): return minus(self, o, swap=1)
+    def __truediv__(self, o): return divide(self, o)
+    def __rtruediv__(self, o): return divide(self, o, swap=1)
+    def __gt__(self, o): return gt(self, o)
+    def __lt__(self, o): return lt(self, o)
+    def __ge__(self, o): return ge(self, o)
+    def __le__(self, o): return le(self, o)
+    def __lshift__(self, o): return shiftleft(self, o)
+    def __rshift__(self, o): return shiftright(self, o)
+    def __or__(self, o): return or2(self, o)
+    def __and__(self, o): return and2(self, o)
+    def __xor__(self, o): return xor(self, o)
+
     # -- methods
     def sumover(self, out=None): return sumover(self, out)
     def dsumover(self, out=None): return dsumover(self, out)
@@ -468,6 +482,20 @@ def _biop(name):
 
 plus = _biop("plus")
 mult = _biop("mult")
+minus = _biop("minus")
+divide = _biop("divide")
+gt = _biop("gt")
+lt = _biop("lt")
+le = _biop("le")
+ge = _biop("ge")
+eq = _biop("eq")
+ne = _biop("ne")
+shiftleft = _biop("shiftleft")
+shiftright = _biop("shiftright")
+or2 = _biop("or2")
+and2 = _biop("and2")
+xor = _biop("xor")
+xor2 = xor  # the reference's alias (lib/PDL/Ops.pd:309-313)
 
 
 def inner(a, b, out=None) -> ndarray:

@@ -474,3 +474,91 @@ def test_float64_products_bit_exact_over_the_exponent_range(gpu):
     want = want + 0.0  # the reference's tmp = 0; tmp += a*b turns -0 into +0
     same = (got.view(np.uint64) == want.view(np.uint64)) | (np.isnan(got) & np.isnan(want))
     assert same.all(), f"inner n=1: {(~same).sum()} products differ"
+
+
+def _golden_gpu(case):
+    from helpers import make_input
+    ins = [make_input(s) for s in case["inputs"]]
+    if case.get("view") == "xchg01":
+        ins[0] = ins[0].xchg(0, 1)
+    out = None
+    if "out" in case:
+        kind, dims = case["out"].split(":")
+        dims = [int(d) for d in dims.split(",")]
+        out = (P.zeroes if kind == "zeroes" else P.ones)("double", *dims)
+    if case["op"] == "matmult":
+        return P.matmult(ins[0], ins[1], out)
+    fn = getattr(P, case["op"])
+    if case["op"] in P_BIOPS:
+        return fn(ins[0], ins[1], out, swap=case.get("swap", 0))
+    return fn(*ins, out) if out is not None else fn(*ins)
+
+
+P_BIOPS = {"plus", "mult", "minus", "divide", "gt", "lt", "le", "ge", "eq", "ne",
+           "shiftleft", "shiftright", "or2", "and2", "xor"}
+
+
+def test_golden_vectors_on_the_gpu(gpu):
+    """Every known answer from the reference's own tests, through the GPU
+    library (the oracle passes the same cases in test_oracle_golden.py)."""
+    from helpers import golden_cases
+    from test_oracle_golden import check_result
+    for case in golden_cases():
+        if "expect_error" in case:
+            with pytest.raises(P.PDLError, match=case["expect_error"]):
+                _golden_gpu(case)
+            continue
+        check_result(case, _golden_gpu(case))
+
+
+NEW_BIOPS = ["minus", "divide", "gt", "lt", "le", "ge", "eq", "ne"]
+BIT_OPS = ["shiftleft", "shiftright", "or2", "and2", "xor"]
+
+
+@pytest.mark.parametrize("t", REAL_TYPES)
+@pytest.mark.parametrize("op", NEW_BIOPS + BIT_OPS)
+def test_more_binary_ops_exact(gpu, op, t):
+    """The other binary ops of Ops.pd against the oracle, bit-exact, under
+    broadcasting, with swap, a supplied output and bad values.  Integer
+    divisors are nonzero and shift counts in [0, 7] with non-negative
+    values (elsewhere the reference's C has no defined result)."""
+    rng = seeded(hash((op, t)) % 2**32)
+    dt = np.dtype(NP_DTYPES[type_code(t)])
+    for sa, sb in [((37, 5), (37, 5)), ((1, 64), (9, 64)), ((7, 1, 33), (1, 4, 33)), ((1,), (6,))]:
+        a, _ = rand_array(rng, t, sa, -100, 100)
+        b, _ = rand_array(rng, t, sb, -100, 100)
+        if op in BIT_OPS:
+            a = np.abs(a.astype(np.float64)).astype(dt)
+        if op in ("shiftleft", "shiftright"):
+            b = (np.abs(b.astype(np.int64)) % 8).astype(dt)
+        if op == "divide" and dt.kind != "f":
+            b = np.where(b == 0, 1, b).astype(dt)
+        if op == "divide" and dt.kind == "f":
+            b.reshape(-1)[::5] = 0  # IEEE inf / NaN
+        for swap in (0, 1):
+            if swap and op in ("divide", "shiftleft", "shiftright") and dt.kind != "f":
+                continue  # the swapped operand would be a divisor / shift count
+            x, y = to_pdl(a, t), to_pdl(b, t)
+            got = getattr(P, op)(x, y, swap=swap)
+            exp = O.run(op, [x, y], swap=swap)[0]
+            assert_same(got, exp, what=f"{op} {t} {sa}x{sb} swap={swap}")
+    # bad values propagate (bit-exact masks and badflag)
+    a, _ = rand_array(rng, t, (50, 8), -100, 100, bad_frac=0.1)
+    b, _ = rand_array(rng, t, (50, 8), 1, 100)
+    if op in ("shiftleft", "shiftright"):
+        b = (np.abs(b.astype(np.int64)) % 8).astype(dt)
+    if op in BIT_OPS:
+        a = np.where(a == P.default_badvalue(type_code(t)), a, np.abs(a.astype(np.float64))).astype(dt)
+    x, y = to_pdl(a, t, badflag=True), to_pdl(b, t)
+    got = getattr(P, op)(x, y)
+    exp = O.run(op, [x, y])[0]
+    assert_same(got, exp, what=f"{op} {t} bad")
+
+
+@pytest.mark.parametrize("op", BIT_OPS)
+def test_bit_ops_on_floats_work_in_longlong(gpu, op):
+    x, y = P.pdl(np.array([1.0, 2.0, 3.0])), P.pdl(np.array([4.0, 5.0, 1.0]))
+    got = getattr(P, op)(x, y)
+    exp = O.run(op, [x, y])[0]
+    assert got.type == "longlong"
+    assert_same(got, exp, what=op)
