@@ -158,6 +158,19 @@ pdlgb300_error pdlgb300_run_minimum(pdlgb300_ndarray *a, pdlgb300_ndarray *c);
 pdlgb300_error pdlgb300_run_maximum(pdlgb300_ndarray *a, pdlgb300_ndarray *c);
 pdlgb300_error pdlgb300_run_minimum_ind(pdlgb300_ndarray *a, pdlgb300_ndarray *c);
 pdlgb300_error pdlgb300_run_maximum_ind(pdlgb300_ndarray *a, pdlgb300_ndarray *c);
+/* lib/PDL/Ufunc.pd:143-187  a(n); [o]b() in a's type: andover (all good
+ * elements nonzero), orover, xorover (an odd count nonzero), zcover (all
+ * zero), bandover/borover/bxorover (bitwise, integer types; float inputs
+ * work in longlong), firstnonzeroover (the first nonzero good element, else
+ * the last good one).  All bad in bad-value mode gives BAD.               */
+pdlgb300_error pdlgb300_run_andover(pdlgb300_ndarray *a, pdlgb300_ndarray *b);
+pdlgb300_error pdlgb300_run_orover(pdlgb300_ndarray *a, pdlgb300_ndarray *b);
+pdlgb300_error pdlgb300_run_xorover(pdlgb300_ndarray *a, pdlgb300_ndarray *b);
+pdlgb300_error pdlgb300_run_zcover(pdlgb300_ndarray *a, pdlgb300_ndarray *b);
+pdlgb300_error pdlgb300_run_bandover(pdlgb300_ndarray *a, pdlgb300_ndarray *b);
+pdlgb300_error pdlgb300_run_borover(pdlgb300_ndarray *a, pdlgb300_ndarray *b);
+pdlgb300_error pdlgb300_run_bxorover(pdlgb300_ndarray *a, pdlgb300_ndarray *b);
+pdlgb300_error pdlgb300_run_firstnonzeroover(pdlgb300_ndarray *a, pdlgb300_ndarray *b);
 /* lib/PDL/Ops.pd:104-153,288-289  plus/mult: a(); b(); [o]c(); int swap   */
 pdlgb300_error pdlgb300_run_plus(pdlgb300_ndarray *a, pdlgb300_ndarray *b,
                                  pdlgb300_ndarray *c, int swap);

@@ -113,6 +113,8 @@ enum {
   OP_MINIMUM_IND, OP_MAXIMUM_IND, OP_PLUS, OP_MULT, OP_INNER, OP_MATMULT,
   OP_MINUS, OP_DIVIDE, OP_GT, OP_LT, OP_LE, OP_GE, OP_EQ, OP_NE, OP_SHIFTLEFT,
   OP_SHIFTRIGHT, OP_OR2, OP_AND2, OP_XOR,
+  OP_ANDOVER, OP_OROVER, OP_XOROVER, OP_ZCOVER, OP_BANDOVER, OP_BOROVER,
+  OP_BXOROVER, OP_FIRSTNONZEROOVER,
   OP_N
 };
 #define IS_BIOP(op) ((op) == OP_PLUS || (op) == OP_MULT || ((op) >= OP_MINUS && (op) <= OP_XOR))
@@ -164,6 +166,15 @@ static const opdef OPS[OP_N] = {
   {"or2", 3, 2, {"a", "b", "c"}, {0, 0, 0}, {{0}, {0}, {0}}, {0}, 0, -1, 1},
   {"and2", 3, 2, {"a", "b", "c"}, {0, 0, 0}, {{0}, {0}, {0}}, {0}, 0, -1, 1},
   {"xor", 3, 2, {"a", "b", "c"}, {0, 0, 0}, {{0}, {0}, {0}}, {0}, 0, -1, 1},
+  /* lib/PDL/Ufunc.pd:143-187: a(n); [o] b() in the generic type */
+  {"andover", 2, 1, {"a", "b"}, {1, 0}, {{0}, {0}}, {"n"}, 0, -1},
+  {"orover", 2, 1, {"a", "b"}, {1, 0}, {{0}, {0}}, {"n"}, 0, -1},
+  {"xorover", 2, 1, {"a", "b"}, {1, 0}, {{0}, {0}}, {"n"}, 0, -1},
+  {"zcover", 2, 1, {"a", "b"}, {1, 0}, {{0}, {0}}, {"n"}, 0, -1},
+  {"bandover", 2, 1, {"a", "b"}, {1, 0}, {{0}, {0}}, {"n"}, 0, -1, 1},
+  {"borover", 2, 1, {"a", "b"}, {1, 0}, {{0}, {0}}, {"n"}, 0, -1, 1},
+  {"bxorover", 2, 1, {"a", "b"}, {1, 0}, {{0}, {0}}, {"n"}, 0, -1, 1},
+  {"firstnonzeroover", 2, 1, {"a", "b"}, {1, 0}, {{0}, {0}}, {"n"}, 0, -1},
 };
 
 static int find_op(const char *name) {
@@ -565,6 +576,19 @@ typedef void (*body_fn)(octx *c, const int64_t *offs, int64_t n0,
   DEF_OVER(prodover_##SYM, CT, SYM, IP, SYM##_ip, ISF, 1, tmp *= v, tmp == 0)                 \
   DEF_OVER(dprodover_##SYM, CT, SYM, double, D, ISF, 1, tmp *= v, tmp == 0)
 
+/* lib/PDL/Ufunc.pd:143-187 (the reference's `char tmp` of the logical ones
+ * holds the same 0/1 as a tmp of the output type) */
+#define DEF_LOGICS(E, CT, SYM, IP, ISF, UNS)                                              \
+  DEF_OVER(andover_##SYM, CT, SYM, CT, SYM, ISF, 1, tmp = (CT)((tmp != 0) & (v != 0)), !tmp) \
+  DEF_OVER(orover_##SYM, CT, SYM, CT, SYM, ISF, 0, tmp = (CT)((tmp != 0) | (v != 0)), tmp)   \
+  DEF_OVER(xorover_##SYM, CT, SYM, CT, SYM, ISF, 0, tmp = (CT)((tmp != 0) ^ (v != 0)), 0)  \
+  DEF_OVER(zcover_##SYM, CT, SYM, CT, SYM, ISF, 1, tmp = (CT)((tmp != 0) & (v == 0)), !tmp) \
+  DEF_OVER(firstnonzeroover_##SYM, CT, SYM, CT, SYM, ISF, 0, tmp = v, tmp)
+#define DEF_BITOVERS(E, CT, SYM, IP, ISF, UNS)                              \
+  DEF_OVER(bandover_##SYM, CT, SYM, CT, SYM, 0, ~0, tmp &= v, !tmp)         \
+  DEF_OVER(borover_##SYM, CT, SYM, CT, SYM, 0, 0, tmp |= v, !~tmp)          \
+  DEF_OVER(bxorover_##SYM, CT, SYM, CT, SYM, 0, 0, tmp ^= v, 0)
+
 /* the int+ output's value-union member per input type */
 #define A_ip L
 #define B_ip L
@@ -578,6 +602,7 @@ typedef void (*body_fn)(octx *c, const int64_t *offs, int64_t n0,
 #define F_ip F
 #define D_ip D
 O_REAL_TYPES(DEF_SUMS)
+O_REAL_TYPES(DEF_LOGICS)
 
 /* cumusumover: a(n); [o]b(n) */
 #define DEF_CUMU(NAME, TA, SYMA, TB, SYMB, ISFA)                                        \
@@ -722,6 +747,13 @@ O_REAL_TYPES(DEF_BIOPS)
   X(PDLGB300_ULL, uint64_t, P, uint64_t, 0, 1)\
   X(PDLGB300_LL, int64_t, Q, int64_t, 0, 0)
 O_INT_TYPES(DEF_BITOPS)
+O_INT_TYPES(DEF_BITOVERS)
+#define bandover_F NULL
+#define bandover_D NULL
+#define borover_F NULL
+#define borover_D NULL
+#define bxorover_F NULL
+#define bxorover_D NULL
 #define shiftleft_F NULL
 #define shiftleft_D NULL
 #define shiftright_F NULL
@@ -856,6 +888,14 @@ static body_fn pick_body(int op, int t) {
     CASE(OP_OR2, or2)
     CASE(OP_AND2, and2)
     CASE(OP_XOR, xor)
+    CASE(OP_ANDOVER, andover)
+    CASE(OP_OROVER, orover)
+    CASE(OP_XOROVER, xorover)
+    CASE(OP_ZCOVER, zcover)
+    CASE(OP_BANDOVER, bandover)
+    CASE(OP_BOROVER, borover)
+    CASE(OP_BXOROVER, bxorover)
+    CASE(OP_FIRSTNONZEROOVER, firstnonzeroover)
   }
 #undef CASE
   return NULL;

@@ -16,7 +16,8 @@ from .ndarray import (  # noqa: F401
     set_default_badvalue, set_matmult_mode, set_stream, set_timing, sumover,
     sumover_bwd, sumover_mult_plus, sync, zeroes)
 from .ndarray import (  # noqa: F401
-    and2, divide, eq, ge, gt, le, lt, minus, ne, or2, shiftleft, shiftright, xor, xor2)
+    and2, divide, eq, ge, gt, le, lt, minus, ne, or2, shiftleft, shiftright, xor, xor2,
+    andover, bandover, borover, bxorover, firstnonzeroover, orover, xorover, zcover)
 from ._abi import MATMULT_BF16X3, MATMULT_BF16X6, MATMULT_SIMT_EXACT, MATMULT_SIMT_FP32  # noqa: F401
 
 __all__ = [n for n in dir() if not n.startswith("_")]

@@ -116,7 +116,9 @@ enum OpId {
   O_AVERAGE, O_DAVERAGE, O_MINIMUM, O_MAXIMUM, O_MINIMUM_IND, O_MAXIMUM_IND,
   O_PLUS, O_MULT, O_INNER, O_MATMULT, O_SMP,
   O_MINUS, O_DIVIDE, O_GT, O_LT, O_LE, O_GE, O_EQ, O_NE,
-  O_SHIFTLEFT, O_SHIFTRIGHT, O_OR2, O_AND2, O_XOR, O_NOPS
+  O_SHIFTLEFT, O_SHIFTRIGHT, O_OR2, O_AND2, O_XOR,
+  O_ANDOVER, O_OROVER, O_XOROVER, O_ZCOVER, O_BANDOVER, O_BOROVER, O_BXOROVER,
+  O_FIRSTNONZEROOVER, O_NOPS
 };
 
 // binary ops (a(); b(); [o]c(); int swap) and their kernel codes
@@ -192,6 +194,15 @@ const pdlgb300_vtable VT[O_NOPS] = {
     {"or2", 3, 2, 0, 1, N_ABC, RD_000, F_ABC, PT_NONE, ID_NONE, nullptr, INTTYPES},
     {"and2", 3, 2, 0, 1, N_ABC, RD_000, F_ABC, PT_NONE, ID_NONE, nullptr, INTTYPES},
     {"xor", 3, 2, 0, 1, N_ABC, RD_000, F_ABC, PT_NONE, ID_NONE, nullptr, INTTYPES},
+    // lib/PDL/Ufunc.pd:143-187: a(n); [o] b() in a's type
+    {"andover", 2, 1, 1, 0, N_AB, RD_10, F_C, PT_NONE, ID_N0, I_N, GENTYPES},
+    {"orover", 2, 1, 1, 0, N_AB, RD_10, F_C, PT_NONE, ID_N0, I_N, GENTYPES},
+    {"xorover", 2, 1, 1, 0, N_AB, RD_10, F_C, PT_NONE, ID_N0, I_N, GENTYPES},
+    {"zcover", 2, 1, 1, 0, N_AB, RD_10, F_C, PT_NONE, ID_N0, I_N, GENTYPES},
+    {"bandover", 2, 1, 1, 0, N_AB, RD_10, F_C, PT_NONE, ID_N0, I_N, INTTYPES},
+    {"borover", 2, 1, 1, 0, N_AB, RD_10, F_C, PT_NONE, ID_N0, I_N, INTTYPES},
+    {"bxorover", 2, 1, 1, 0, N_AB, RD_10, F_C, PT_NONE, ID_N0, I_N, INTTYPES},
+    {"firstnonzeroover", 2, 1, 1, 0, N_AB, RD_10, F_C, PT_NONE, ID_N0, I_N, GENTYPES},
 };
 
 int op_of(const pdlgb300_vtable *vt) {
@@ -945,7 +956,8 @@ pdlgb300_error dispatch_reduce(RunCtx &c, int redop) {
       int occ = (redop == R_SUM || redop == R_DSUM || redop == R_AVG || redop == R_DAVG)
                     ? red_occ_sum(redop, dt0, a.f32_comp, a.bad, lc.block)
                 : (redop == R_PROD || redop == R_DPROD) ? red_occ_prod(redop, dt0, a.bad, lc.block)
-                                                        : red_occ_minmax(redop, dt0, a.bad, lc.block);
+                : red_is_logic(redop) ? red_occ_logic(redop, dt0, a.bad, lc.block)
+                                      : red_occ_minmax(redop, dt0, a.bad, lc.block);
       const int64_t slots = (int64_t)nsm * occ;
       int64_t want = std::max<int64_t>(1, slots / a.rows);
       int64_t maxs = a.n / 8192;
@@ -960,7 +972,8 @@ pdlgb300_error dispatch_reduce(RunCtx &c, int redop) {
   const bool zfix = lc.kind == 0 && (redop == R_DPROD ||
                                      (redop == R_PROD && (dtin == PDLGB300_F || dtin == PDLGB300_D)));
   if (a.nsplit > 1 || zfix) {
-    size_t accsz = red_acc_size(redop, dtin, a.f32_comp);
+    size_t accsz = red_is_logic(redop) ? red_acc_size_logic(redop, dtin)
+                                       : red_acc_size(redop, dtin, a.f32_comp);
     size_t npart = a.nsplit > 1 ? (size_t)a.rows * a.nsplit : 0;
     size_t off = (npart * accsz + 15) & ~(size_t)15;
     size_t offz = off + ((npart * sizeof(int64_t) + 15) & ~(size_t)15);
@@ -981,6 +994,8 @@ pdlgb300_error dispatch_reduce(RunCtx &c, int redop) {
     e = launch_red_sum(redop, dt, a, lc, g_stream);
   else if (redop == R_PROD || redop == R_DPROD)
     e = launch_red_prod(redop, dt, a, lc, g_stream);
+  else if (red_is_logic(redop))
+    e = launch_red_logic(redop, dt, a, lc, g_stream);
   else
     e = launch_red_minmax(redop, dt, a, lc, g_stream);
   if (scratch) cudaFreeAsync(scratch, g_stream);
@@ -1281,6 +1296,14 @@ pdlgb300_error dispatch(RunCtx &c, const int64_t *) {
     case O_GE: case O_EQ: case O_NE: case O_SHIFTLEFT: case O_SHIFTRIGHT: case O_OR2:
     case O_AND2: case O_XOR:
       return dispatch_biop(c, biop_code_of(c.op));
+    case O_ANDOVER: return dispatch_reduce(c, R_AND);
+    case O_OROVER: return dispatch_reduce(c, R_OR);
+    case O_XOROVER: return dispatch_reduce(c, R_XOR);
+    case O_ZCOVER: return dispatch_reduce(c, R_ZC);
+    case O_BANDOVER: return dispatch_reduce(c, R_BAND);
+    case O_BOROVER: return dispatch_reduce(c, R_BOR);
+    case O_BXOROVER: return dispatch_reduce(c, R_BXOR);
+    case O_FIRSTNONZEROOVER: return dispatch_reduce(c, R_FIRSTNZ);
     case O_INNER: return dispatch_inner(c);
     case O_MATMULT: return dispatch_matmult(c);
     case O_SMP: return dispatch_smp(c);
@@ -1407,6 +1430,14 @@ RUN2(minimum, O_MINIMUM)
 RUN2(maximum, O_MAXIMUM)
 RUN2(minimum_ind, O_MINIMUM_IND)
 RUN2(maximum_ind, O_MAXIMUM_IND)
+RUN2(andover, O_ANDOVER)
+RUN2(orover, O_OROVER)
+RUN2(xorover, O_XOROVER)
+RUN2(zcover, O_ZCOVER)
+RUN2(bandover, O_BANDOVER)
+RUN2(borover, O_BOROVER)
+RUN2(bxorover, O_BXOROVER)
+RUN2(firstnonzeroover, O_FIRSTNONZEROOVER)
 
 pdlgb300_error pdlgb300_run_plus(pdlgb300_ndarray *a, pdlgb300_ndarray *b, pdlgb300_ndarray *c,
                                  int swap) {

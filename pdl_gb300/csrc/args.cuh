@@ -13,8 +13,11 @@ template <class T> __host__ __device__ __forceinline__ T from_bits(uint64_t b) {
 // ------------------------------------------------------------ reductions
 enum RedOp {
   R_SUM = 0, R_DSUM, R_PROD, R_DPROD, R_AVG, R_DAVG, R_MIN, R_MAX,
-  R_MIN_IND, R_MAX_IND, R_NOPS
+  R_MIN_IND, R_MAX_IND,
+  // lib/PDL/Ufunc.pd:143-187
+  R_AND, R_OR, R_XOR, R_ZC, R_BAND, R_BOR, R_BXOR, R_FIRSTNZ, R_NOPS
 };
+inline bool red_is_logic(int op) { return op >= R_AND && op <= R_FIRSTNZ; }
 
 struct RedArgs {
   const char *a;      // element (0) of a (already offset)
@@ -48,6 +51,10 @@ pdlgb300_error launch_red_prod(int op, int in_dt, RedArgs args, const RedLaunch 
                                cudaStream_t s);
 pdlgb300_error launch_red_minmax(int op, int in_dt, RedArgs args, const RedLaunch &lc,
                                  cudaStream_t s);
+pdlgb300_error launch_red_logic(int op, int in_dt, RedArgs args, const RedLaunch &lc,
+                                cudaStream_t s);
+int red_occ_logic(int op, int in_dt, bool bad, int block);
+size_t red_acc_size_logic(int op, int in_dt);
 size_t red_acc_size(int op, int in_dt, int f32_comp);
 int red_occ_sum(int op, int in_dt, int comp, bool bad, int block);
 int red_occ_prod(int op, int in_dt, bool bad, int block);

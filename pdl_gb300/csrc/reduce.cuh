@@ -255,6 +255,102 @@ template <class T, bool MAX, bool IND> struct OpMM {
   }
 };
 
+// Logical and bitwise reductions (lib/PDL/Ufunc.pd:143-187), all order free:
+// K 0 andover (tmp &= a != 0), 1 orover, 2 xorover, 3 zcover (tmp &= a == 0),
+// 4 bandover (tmp &= a), 5 borover, 6 bxorover.  The reference stops early
+// once the result cannot change (its leftzero); that changes no result.
+// A bad element is replaced by the op's neutral element; no good element
+// in bad-value mode gives BAD.
+template <class T, int K> struct OpLogic {
+  static constexpr bool kBits = K >= 4 && std::is_integral_v<T>;
+  // bit ops work on the unsigned image, widened to 4 bytes for the shuffles
+  // (the low bits, which is all the result keeps, are the same)
+  using Acc = std::conditional_t<kBits && (sizeof(T) >= 4), uns_t<T>, uint32_t>;
+  static constexpr bool kCount = false, kVec = true, kBlock = false, kNeutral = true;
+  static constexpr bool kZero = false, kLeftZero = false;
+  static constexpr int kU = 0;
+  __device__ static T neutral() {
+    if constexpr (K == 0) return (T)1;  // a != 0 leaves "and" as it is
+    else if constexpr (K == 4 && kBits) return (T)(~(uns_t<T>)0);
+    else return (T)0;
+  }
+  template <int VEC, int U>
+  __device__ static void add_block(Acc &, const T *, int64_t, int64_t) {}
+  __device__ static Acc init() {
+    if constexpr (K == 0 || K == 3) return 1;
+    else if constexpr (K == 4) return (Acc)(~(Acc)0);
+    else return 0;
+  }
+  __device__ static void add(Acc &a, T v, int64_t) {
+    if constexpr (K == 0) a &= (Acc)(v != (T)0);
+    else if constexpr (K == 1) a |= (Acc)(v != (T)0);
+    else if constexpr (K == 2) a ^= (Acc)(v != (T)0);
+    else if constexpr (K == 3) a &= (Acc)(v == (T)0);
+    else if constexpr (K == 4) a &= (Acc)v;
+    else if constexpr (K == 5) a |= (Acc)v;
+    else a ^= (Acc)v;
+  }
+  template <int VEC> __device__ static void add_vec(Acc &a, const T *v, int64_t i) {
+#pragma unroll
+    for (int e = 0; e < VEC; e++) add(a, v[e], i + e);
+  }
+  __device__ static void merge(Acc &a, const Acc &b) {
+    if constexpr (K == 0 || K == 3 || K == 4) a &= b;
+    else if constexpr (K == 1 || K == 5) a |= b;
+    else a ^= b;
+  }
+  __device__ static T fin(const Acc &a, int64_t cnt, bool bad, T badval, int *) {
+    if (bad && cnt == 0) return badval;
+    return (T)a;
+  }
+};
+
+// firstnonzeroover (lib/PDL/Ufunc.pd:144-145): `tmp = a` until tmp is
+// nonzero, so the first nonzero good element, else the last good element
+// (a zero, with its sign), else 0 (n == 0) or BAD (all bad).
+template <class T> struct OpFirstNZ {
+  struct Acc {
+    int64_t nz;    // index of the first nonzero seen, INT64_MAX: none
+    int64_t last;  // index of the last good element seen, -1: none
+    T nzv, lastv;
+  };
+  static constexpr bool kCount = false, kVec = true, kBlock = false, kNeutral = false;
+  static constexpr bool kZero = false, kLeftZero = false;
+  static constexpr int kU = 8;
+  __device__ static T neutral() { return (T)0; }
+  template <int VEC, int U>
+  __device__ static void add_block(Acc &, const T *, int64_t, int64_t) {}
+  __device__ static Acc init() { return Acc{INT64_MAX, -1, (T)0, (T)0}; }
+  __device__ static void add(Acc &a, T v, int64_t i) {
+    if (v != (T)0 && i < a.nz) {  // NaN is nonzero, as in C
+      a.nz = i;
+      a.nzv = v;
+    }
+    if (i > a.last) {
+      a.last = i;
+      a.lastv = v;
+    }
+  }
+  template <int VEC> __device__ static void add_vec(Acc &a, const T *v, int64_t i) {
+#pragma unroll
+    for (int e = 0; e < VEC; e++) add(a, v[e], i + e);
+  }
+  __device__ static void merge(Acc &a, const Acc &b) {
+    if (b.nz < a.nz) {
+      a.nz = b.nz;
+      a.nzv = b.nzv;
+    }
+    if (b.last > a.last) {
+      a.last = b.last;
+      a.lastv = b.lastv;
+    }
+  }
+  __device__ static T fin(const Acc &a, int64_t, bool bad, T badval, int *) {
+    if (a.last < 0) return bad ? badval : (T)0;
+    return a.nz != INT64_MAX ? a.nzv : a.lastv;
+  }
+};
+
 // float64 minimum/maximum(+_ind) on the integer pipe.  GB300 retires about
 // 2 FP64 instructions per clock per SM, so FP64 compares cannot keep up
 // with HBM; instead each double maps to an ordered int64 key (sign-magnitude

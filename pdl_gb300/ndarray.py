@@ -464,6 +464,14 @@ average = _red("average")
 daverage = _red("daverage")
 minimum = _red("minimum")
 maximum = _red("maximum")
+andover = _red("andover")
+orover = _red("orover")
+xorover = _red("xorover")
+zcover = _red("zcover")
+bandover = _red("bandover")
+borover = _red("borover")
+bxorover = _red("bxorover")
+firstnonzeroover = _red("firstnonzeroover")
 minimum_ind = _red("minimum_ind")
 maximum_ind = _red("maximum_ind")
 avgover, minover, maxover = average, minimum, maximum

@@ -562,3 +562,38 @@ def test_bit_ops_on_floats_work_in_longlong(gpu, op):
     exp = O.run(op, [x, y])[0]
     assert got.type == "longlong"
     assert_same(got, exp, what=op)
+
+
+LOGIC_OPS = ["andover", "orover", "xorover", "zcover", "firstnonzeroover"]
+BITOVER_OPS = ["bandover", "borover", "bxorover"]
+
+
+@pytest.mark.parametrize("t", REAL_TYPES)
+@pytest.mark.parametrize("op", LOGIC_OPS + BITOVER_OPS)
+def test_logical_and_bitwise_reductions(gpu, op, t):
+    """Ufunc.pd:143-187 against the oracle, bit-exact: sparse zeros so the
+    logical results vary, rows of every kernel path (warp rows, block rows,
+    split long rows, strided views), bad values with all-bad rows."""
+    rng = seeded(hash((op, t, "logic")) % 2**32)
+    for shape in [(7,), (0,), (3, 0), (33, 17), (2049, 6), (300_000, 2)]:
+        a, _ = rand_array(rng, t, shape[::-1], -3, 3)
+        x = to_pdl(a, t)
+        got, exp = _run_both(op, [x])
+        assert_same(got, exp, what=f"{op} {t} {shape}")
+    a, _ = rand_array(rng, t, (30, 40, 5), -3, 3)
+    got, exp = _run_both(op, [to_pdl(a, t).xchg(0, 1)])
+    assert_same(got, exp, what=f"{op} {t} strided")
+    a, bad = rand_array(rng, t, (12, 900), -3, 3, bad_frac=0.3)
+    a[0, :] = P.default_badvalue(type_code(t))
+    got, exp = _run_both(op, [to_pdl(a, t, badflag=True)])
+    assert_same(got, exp, what=f"{op} {t} bad")
+
+
+def test_firstnonzeroover_zero_rows_keep_the_last_zero(gpu):
+    a = np.array([[0.0, -0.0, 0.0, -0.0], [0.0, 0.0, -0.0, 3.0], [np.nan, 1.0, 0.0, 0.0]])
+    x = P.pdl(a)
+    got, exp = _run_both("firstnonzeroover", [x])
+    g, e = got.numpy(), exp.numpy()
+    assert np.array_equal(np.isnan(g), np.isnan(e))
+    assert np.array_equal(g[~np.isnan(g)], e[~np.isnan(e)])
+    assert np.array_equal(np.signbit(g), np.signbit(e))
