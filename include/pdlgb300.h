@@ -171,6 +171,11 @@ pdlgb300_error pdlgb300_run_bandover(pdlgb300_ndarray *a, pdlgb300_ndarray *b);
 pdlgb300_error pdlgb300_run_borover(pdlgb300_ndarray *a, pdlgb300_ndarray *b);
 pdlgb300_error pdlgb300_run_bxorover(pdlgb300_ndarray *a, pdlgb300_ndarray *b);
 pdlgb300_error pdlgb300_run_firstnonzeroover(pdlgb300_ndarray *a, pdlgb300_ndarray *b);
+/* lib/PDL/Ufunc.pd:120-140  cumuprodover: a(n); int+ [o]b(n), the running
+ * product (a bad element gives a bad output and leaves the product as it
+ * is); dcumuprodover: double [o]b(n).                                     */
+pdlgb300_error pdlgb300_run_cumuprodover(pdlgb300_ndarray *a, pdlgb300_ndarray *b);
+pdlgb300_error pdlgb300_run_dcumuprodover(pdlgb300_ndarray *a, pdlgb300_ndarray *b);
 /* lib/PDL/Ops.pd:104-153,288-289  plus/mult: a(); b(); [o]c(); int swap   */
 pdlgb300_error pdlgb300_run_plus(pdlgb300_ndarray *a, pdlgb300_ndarray *b,
                                  pdlgb300_ndarray *c, int swap);

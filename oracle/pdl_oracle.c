@@ -114,7 +114,7 @@ enum {
   OP_MINUS, OP_DIVIDE, OP_GT, OP_LT, OP_LE, OP_GE, OP_EQ, OP_NE, OP_SHIFTLEFT,
   OP_SHIFTRIGHT, OP_OR2, OP_AND2, OP_XOR,
   OP_ANDOVER, OP_OROVER, OP_XOROVER, OP_ZCOVER, OP_BANDOVER, OP_BOROVER,
-  OP_BXOROVER, OP_FIRSTNONZEROOVER,
+  OP_BXOROVER, OP_FIRSTNONZEROOVER, OP_CUMUPRODOVER, OP_DCUMUPRODOVER,
   OP_N
 };
 #define IS_BIOP(op) ((op) == OP_PLUS || (op) == OP_MULT || ((op) >= OP_MINUS && (op) <= OP_XOR))
@@ -175,6 +175,8 @@ static const opdef OPS[OP_N] = {
   {"borover", 2, 1, {"a", "b"}, {1, 0}, {{0}, {0}}, {"n"}, 0, -1, 1},
   {"bxorover", 2, 1, {"a", "b"}, {1, 0}, {{0}, {0}}, {"n"}, 0, -1, 1},
   {"firstnonzeroover", 2, 1, {"a", "b"}, {1, 0}, {{0}, {0}}, {"n"}, 0, -1},
+  {"cumuprodover", 2, 1, {"a", "b"}, {1, 1}, {{0}, {0}}, {"n"}, TYPED | TPLUS, PDLGB300_L},
+  {"dcumuprodover", 2, 1, {"a", "b"}, {1, 1}, {{0}, {0}}, {"n"}, TYPED, PDLGB300_D},
 };
 
 static int find_op(const char *name) {
@@ -605,7 +607,8 @@ O_REAL_TYPES(DEF_SUMS)
 O_REAL_TYPES(DEF_LOGICS)
 
 /* cumusumover: a(n); [o]b(n) */
-#define DEF_CUMU(NAME, TA, SYMA, TB, SYMB, ISFA)                                        \
+#define DEF_CUMU(NAME, TA, SYMA, TB, SYMB, ISFA) DEF_CUMU_OP(NAME, TA, SYMA, TB, SYMB, ISFA, 0, +=)
+#define DEF_CUMU_OP(NAME, TA, SYMA, TB, SYMB, ISFA, INIT, OP)                          \
   static void NAME(octx *c, const int64_t *offs, int64_t n0, const int64_t *inc0) { \
     int64_t N = c->ind_sizes[0], ia = c->inc_sizes[0][0], ib = c->inc_sizes[1][0];   \
     TA abad = c->bad[0].SYMA;                                                        \
@@ -613,21 +616,23 @@ O_REAL_TYPES(DEF_LOGICS)
     for (int64_t i0 = 0; i0 < n0; i0++) {                                            \
       const TA *a = (const TA *)c->base[0] + offs[0] + i0 * inc0[0];                 \
       TB *b = (TB *)c->base[1] + offs[1] + i0 * inc0[1];                             \
-      TB tmp = 0;                                                                    \
+      TB tmp = INIT;                                                                 \
       for (int64_t n = 0; n < N; n++) {                                              \
         TA v = a[n * ia];                                                            \
         if (c->bvalflag && ISBADV(v, abad, ISFA)) {                                  \
           b[n * ib] = bbad;                                                          \
           continue;                                                                  \
         }                                                                            \
-        tmp += v;                                                                    \
+        tmp OP v;                                                                    \
         b[n * ib] = tmp;                                                             \
       }                                                                              \
     }                                                                                \
   }
-#define DEF_CUMUS(E, CT, SYM, IP, ISF, UNS)              \
-  DEF_CUMU(cumusumover_##SYM, CT, SYM, IP, SYM##_ip, ISF) \
-  DEF_CUMU(dcumusumover_##SYM, CT, SYM, double, D, ISF)
+#define DEF_CUMUS(E, CT, SYM, IP, ISF, UNS)                           \
+  DEF_CUMU(cumusumover_##SYM, CT, SYM, IP, SYM##_ip, ISF)              \
+  DEF_CUMU(dcumusumover_##SYM, CT, SYM, double, D, ISF)                \
+  DEF_CUMU_OP(cumuprodover_##SYM, CT, SYM, IP, SYM##_ip, ISF, 1, *=)   \
+  DEF_CUMU_OP(dcumuprodover_##SYM, CT, SYM, double, D, ISF, 1, *=)
 O_REAL_TYPES(DEF_CUMUS)
 
 /* average: tmp/cnt with cnt a PDL_Indx (C's usual conversions) */
@@ -896,6 +901,8 @@ static body_fn pick_body(int op, int t) {
     CASE(OP_BOROVER, borover)
     CASE(OP_BXOROVER, bxorover)
     CASE(OP_FIRSTNONZEROOVER, firstnonzeroover)
+    CASE(OP_CUMUPRODOVER, cumuprodover)
+    CASE(OP_DCUMUPRODOVER, dcumuprodover)
   }
 #undef CASE
   return NULL;

@@ -96,7 +96,7 @@ SIGNATURES = {
     "pdlgb300_run_minimum_ind": (Error, [P, P]),
     **{f"pdlgb300_run_{op}": (Error, [P, P])
        for op in ("andover", "orover", "xorover", "zcover", "bandover", "borover",
-                  "bxorover", "firstnonzeroover")},
+                  "bxorover", "firstnonzeroover", "cumuprodover", "dcumuprodover")},
     "pdlgb300_run_maximum_ind": (Error, [P, P]),
     "pdlgb300_run_plus": (Error, [P, P, P, C.c_int]),
     "pdlgb300_run_mult": (Error, [P, P, P, C.c_int]),

@@ -118,7 +118,7 @@ enum OpId {
   O_MINUS, O_DIVIDE, O_GT, O_LT, O_LE, O_GE, O_EQ, O_NE,
   O_SHIFTLEFT, O_SHIFTRIGHT, O_OR2, O_AND2, O_XOR,
   O_ANDOVER, O_OROVER, O_XOROVER, O_ZCOVER, O_BANDOVER, O_BOROVER, O_BXOROVER,
-  O_FIRSTNONZEROOVER, O_NOPS
+  O_FIRSTNONZEROOVER, O_CUMUPRODOVER, O_DCUMUPRODOVER, O_NOPS
 };
 
 // binary ops (a(); b(); [o]c(); int swap) and their kernel codes
@@ -203,6 +203,9 @@ const pdlgb300_vtable VT[O_NOPS] = {
     {"borover", 2, 1, 1, 0, N_AB, RD_10, F_C, PT_NONE, ID_N0, I_N, INTTYPES},
     {"bxorover", 2, 1, 1, 0, N_AB, RD_10, F_C, PT_NONE, ID_N0, I_N, INTTYPES},
     {"firstnonzeroover", 2, 1, 1, 0, N_AB, RD_10, F_C, PT_NONE, ID_N0, I_N, GENTYPES},
+    // lib/PDL/Ufunc.pd:120-140 with `*=`: a(n); int+ [o]b(n) / double [o]b(n)
+    {"cumuprodover", 2, 1, 1, 0, N_AB, RD_11, F_TP, PT_L, ID_NN, I_N, GENTYPES},
+    {"dcumuprodover", 2, 1, 1, 0, N_AB, RD_11, F_T, PT_D, ID_NN, I_N, REALTYPES},
 };
 
 int op_of(const pdlgb300_vtable *vt) {
@@ -1304,6 +1307,8 @@ pdlgb300_error dispatch(RunCtx &c, const int64_t *) {
     case O_BOROVER: return dispatch_reduce(c, R_BOR);
     case O_BXOROVER: return dispatch_reduce(c, R_BXOR);
     case O_FIRSTNONZEROOVER: return dispatch_reduce(c, R_FIRSTNZ);
+    case O_CUMUPRODOVER: return dispatch_cumusum(c, 2);
+    case O_DCUMUPRODOVER: return dispatch_cumusum(c, 3);
     case O_INNER: return dispatch_inner(c);
     case O_MATMULT: return dispatch_matmult(c);
     case O_SMP: return dispatch_smp(c);
@@ -1438,6 +1443,8 @@ RUN2(bandover, O_BANDOVER)
 RUN2(borover, O_BOROVER)
 RUN2(bxorover, O_BXOROVER)
 RUN2(firstnonzeroover, O_FIRSTNONZEROOVER)
+RUN2(cumuprodover, O_CUMUPRODOVER)
+RUN2(dcumuprodover, O_DCUMUPRODOVER)
 
 pdlgb300_error pdlgb300_run_plus(pdlgb300_ndarray *a, pdlgb300_ndarray *b, pdlgb300_ndarray *c,
                                  int swap) {

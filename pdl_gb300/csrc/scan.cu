@@ -30,24 +30,46 @@ __device__ __forceinline__ FF2 ff2_add(FF2 a, FF2 b) {
   return FF2{h, __fsub_rn(e, __fsub_rn(h, s))};
 }
 
-// Running-sum arithmetic in Out's type.
-template <class In, class Out, bool COMP> struct ScanT {
+// Running arithmetic in Out's type.  M: 0 sum, 1 compensated float32 sum,
+// 2 product (cumuprodover, lib/PDL/Ufunc.pd:120-140 with `*=`).  zero() is
+// the identity; pad() the input value that changes nothing.
+template <class In, class Out, int M> struct ScanT {
+  static constexpr bool kProd = M == 2;
   using Acc = std::conditional_t<std::is_integral_v<Out>, uns_t<Out>,
-                                 std::conditional_t<std::is_same_v<Out, float> && COMP, FF2, Out>>;
+                                 std::conditional_t<std::is_same_v<Out, float> && M == 1, FF2, Out>>;
   __device__ static Acc zero() {
     Acc a;
-    memset(&a, 0, sizeof a);
+    if constexpr (kProd) {
+      a = (Acc)1;
+    } else {
+      memset(&a, 0, sizeof a);
+    }
     return a;
   }
+  __device__ static In pad() { return kProd ? (In)1 : (In)0; }
   __device__ static Acc add1(Acc a, In v) {
-    if constexpr (std::is_integral_v<Out>) return a + (Acc)(Out)v;
-    else if constexpr (std::is_same_v<Acc, FF2>) return ff2_add1(a, (float)v);
-    else return rn_add(a, (Out)v);
+    if constexpr (kProd) {
+      if constexpr (std::is_integral_v<Out>) return (Acc)wmul<Out>((Out)a, (Out)v);
+      else return rn_mul(a, (Out)v);
+    } else if constexpr (std::is_integral_v<Out>) {
+      return a + (Acc)(Out)v;
+    } else if constexpr (std::is_same_v<Acc, FF2>) {
+      return ff2_add1(a, (float)v);
+    } else {
+      return rn_add(a, (Out)v);
+    }
   }
   __device__ static Acc add(Acc a, Acc b) {
-    if constexpr (std::is_integral_v<Out>) return a + b;
-    else if constexpr (std::is_same_v<Acc, FF2>) return ff2_add(a, b);
-    else return rn_add(a, b);
+    if constexpr (kProd) {
+      if constexpr (std::is_integral_v<Out>) return (Acc)wmul<Out>((Out)a, (Out)b);
+      else return rn_mul(a, b);
+    } else if constexpr (std::is_integral_v<Out>) {
+      return a + b;
+    } else if constexpr (std::is_same_v<Acc, FF2>) {
+      return ff2_add(a, b);
+    } else {
+      return rn_add(a, b);
+    }
   }
   __device__ static Out value(Acc a) {
     if constexpr (std::is_integral_v<Out>) return (Out)a;
@@ -93,7 +115,7 @@ constexpr int SB = 256, SI = 8, STILE = SB * SI;
 // in registers.  Long rows with few rows are cut into chunks: chunk totals
 // first (mode 1), then each chunk scanned from the sum of its row's earlier
 // chunk totals, which its warp adds up itself (mode 2).
-template <class In, class Out, bool BAD, bool COMP>
+template <class In, class Out, bool BAD, int COMP>
 __global__ void __launch_bounds__(256) k_scan_warp(const ScanArgs g) {
   using S = ScanT<In, Out, COMP>;
   using Acc = typename S::Acc;
@@ -150,7 +172,7 @@ __global__ void __launch_bounds__(256) k_scan_warp(const ScanArgs g) {
 #pragma unroll
       for (int j = 0; j < PER; j++) good[j] = base + j < hi && !(BAD && bv.is(cur[j]));
       Acc tot = S::zero();
-      if constexpr (std::is_same_v<Out, double> && std::is_same_v<In, double> && !BAD) {
+      if constexpr (std::is_same_v<Out, double> && std::is_same_v<In, double> && !BAD && !S::kProd) {
         F64Sum fs{0.0};
         double w[PER];
 #pragma unroll
@@ -330,7 +352,7 @@ __device__ __forceinline__ Acc chain_lookback(const ScanArgs &g, ChainSlot *slot
 // across the block barriers and more blocks fit on an SM to cover the
 // look-back latency.  Equal-width outputs overwrite their input slots; wider
 // outputs (float32 -> float64) use a second, larger tile.
-template <class In, class Out, int BM, bool COMP>
+template <class In, class Out, int BM, int COMP>
 __global__ void __launch_bounds__(chain_threads<In, Out>(), (sizeof(In) == 4 && sizeof(Out) == 4) ? 3 : 4)
     k_scan_chain(const ScanArgs g, int64_t u0) {
   constexpr int CB = chain_threads<In, Out>();
@@ -395,7 +417,7 @@ __global__ void __launch_bounds__(chain_threads<In, Out>(), (sizeof(In) == 4 && 
     for (int q = 0; q < NV; q++) {
       In x[VEC];
 #pragma unroll
-      for (int e = 0; e < VEC; e++) x[e] = q * VEC + e < nvalid ? a[t0 + q * VEC + e] : (In)0;
+      for (int e = 0; e < VEC; e++) x[e] = q * VEC + e < nvalid ? a[t0 + q * VEC + e] : S::pad();
       float4 f;
       memcpy(&f, x, 16);
       asm volatile("st.shared.v4.f32 [%0], {%1,%2,%3,%4};" ::"r"(slot_in(q)), "f"(f.x),
@@ -403,12 +425,12 @@ __global__ void __launch_bounds__(chain_threads<In, Out>(), (sizeof(In) == 4 && 
                    : "memory");
     }
   }
-  // items past the row's end hold 0, which adds nothing and is never stored
+  // items past the row's end hold the identity and are never stored
   auto good = [&](In x) { return !is_bad<In, BM>(x, bad); };
 
   // thread total
   Acc tot = S::zero();
-  if constexpr (std::is_same_v<In, double> && std::is_same_v<Out, double>) {
+  if constexpr (std::is_same_v<In, double> && std::is_same_v<Out, double> && !S::kProd) {
     // float64: two exact 8-element blocks (integer alignment, one FP64 add each)
     F64Sum fs{0.0};
 #pragma unroll
@@ -536,7 +558,7 @@ __global__ void __launch_bounds__(chain_threads<In, Out>(), (sizeof(In) == 4 && 
 }
 
 // One thread per row, any increments, the reference's order.
-template <class In, class Out, bool BAD, bool COMP>
+template <class In, class Out, bool BAD, int COMP>
 __global__ void k_scan_thread(const ScanArgs g) {
   using S = ScanT<In, Out, COMP>;
   Bad<In> bv{from_bits<In>(g.abad), (bool)g.abad_isnan};
@@ -565,7 +587,7 @@ template <class In, class Out> constexpr bool chain_ok() {
          (sizeof(Out) == sizeof(In) || sizeof(Out) == 2 * sizeof(In));
 }
 
-template <class In, class Out, bool COMP>
+template <class In, class Out, int COMP>
 pdlgb300_error scan_chain_typed(ScanArgs g, cudaStream_t s) {
   pdlgb300_error e = pgh::ok();
   if constexpr (chain_ok<In, Out>()) {
@@ -608,7 +630,7 @@ template <class In, class Out> constexpr int64_t chain_chunk() {
   return 0;
 }
 
-template <class In, class Out, bool COMP>
+template <class In, class Out, int COMP>
 pdlgb300_error scan_typed(ScanArgs g, cudaStream_t s) {
   pdlgb300_error e = pgh::ok();
   if (g.rows == 0) return e;
@@ -647,15 +669,18 @@ pdlgb300_error scan_typed(ScanArgs g, cudaStream_t s) {
 
 }  // namespace
 
-// dop: 0 cumusumover (int+), 1 dcumusumover (double)
+// dop: 0 cumusumover (int+), 1 dcumusumover (double), 2 cumuprodover
+// (int+), 3 dcumuprodover (double)
 pdlgb300_error launch_cumusum(int dop, int in_dt, ScanArgs g, cudaStream_t s) {
   PG_DISPATCH(in_dt, {
     using In = typename TT<DT>::T;
     using OutP = typename TT<intplus(DT)>::T;
-    if (dop == 1) return scan_typed<In, double, false>(g, s);
+    if (dop == 1) return scan_typed<In, double, 0>(g, s);
+    if (dop == 2) return scan_typed<In, OutP, 2>(g, s);
+    if (dop == 3) return scan_typed<In, double, 2>(g, s);
     if constexpr (std::is_same_v<OutP, float>)
-      if (g.f32_comp) return scan_typed<In, OutP, true>(g, s);
-    return scan_typed<In, OutP, false>(g, s);
+      if (g.f32_comp) return scan_typed<In, OutP, 1>(g, s);
+    return scan_typed<In, OutP, 0>(g, s);
   });
   return pgh::err(PDLGB300_EUSERERROR, "cumusumover: unsupported type %d", in_dt);
 }
@@ -666,7 +691,7 @@ int64_t scan_chain_chunk(int dop, int in_dt, int comp) {
     using In = typename TT<DT>::T;
     using OutP = typename TT<intplus(DT)>::T;
     (void)comp;
-    if (dop == 1) r = chain_chunk<In, double>();
+    if (dop == 1 || dop == 3) r = chain_chunk<In, double>();
     else r = chain_chunk<In, OutP>();
   });
   return r;
@@ -677,9 +702,11 @@ size_t scan_acc_size(int dop, int in_dt, int comp) {
   PG_DISPATCH(in_dt, {
     using In = typename TT<DT>::T;
     using OutP = typename TT<intplus(DT)>::T;
-    if (dop == 1) r = sizeof(typename ScanT<In, double, false>::Acc);
-    else if (comp) r = sizeof(typename ScanT<In, OutP, true>::Acc);
-    else r = sizeof(typename ScanT<In, OutP, false>::Acc);
+    if (dop == 1) r = sizeof(typename ScanT<In, double, 0>::Acc);
+    else if (dop == 2) r = sizeof(typename ScanT<In, OutP, 2>::Acc);
+    else if (dop == 3) r = sizeof(typename ScanT<In, double, 2>::Acc);
+    else if (comp) r = sizeof(typename ScanT<In, OutP, 1>::Acc);
+    else r = sizeof(typename ScanT<In, OutP, 0>::Acc);
   });
   return r;
 }

@@ -472,6 +472,8 @@ bandover = _red("bandover")
 borover = _red("borover")
 bxorover = _red("bxorover")
 firstnonzeroover = _red("firstnonzeroover")
+cumuprodover = _red("cumuprodover")
+dcumuprodover = _red("dcumuprodover")
 minimum_ind = _red("minimum_ind")
 maximum_ind = _red("maximum_ind")
 avgover, minover, maxover = average, minimum, maximum

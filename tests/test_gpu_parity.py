@@ -42,7 +42,7 @@ def _tol(op, x_np, exp, out_type):
         return (n + 2) * eps, 1e-300, scale
     if op in ("cumusumover", "dcumusumover"):
         return (n + 2) * eps, 1e-300, np.cumsum(a, axis=-1)
-    if op in ("prodover", "dprodover"):
+    if op in ("prodover", "dprodover", "cumuprodover", "dcumuprodover"):
         return (n + 2) * eps, 1e-290 if acc == "double" else 1e-36, None
     return 0.0, 0.0, None
 
@@ -597,3 +597,34 @@ def test_firstnonzeroover_zero_rows_keep_the_last_zero(gpu):
     assert np.array_equal(np.isnan(g), np.isnan(e))
     assert np.array_equal(g[~np.isnan(g)], e[~np.isnan(e)])
     assert np.array_equal(np.signbit(g), np.signbit(e))
+
+
+@pytest.mark.parametrize("t", REAL_TYPES)
+@pytest.mark.parametrize("op", ["cumuprodover", "dcumuprodover"])
+def test_running_products(gpu, op, t):
+    """cumuprodover (Ufunc.pd:120-140 with *=) against the oracle: integers
+    wrap exactly whatever the order; floats near 1 in magnitude (no
+    underflow or overflow on the way) within (n+2) eps |p|; rows of every
+    scan path (thread rows, warp rows, the chained scan over many chunks),
+    bad values."""
+    rng = seeded(hash((op, t, "cumuprod")) % 2**32)
+    dt = np.dtype(NP_DTYPES[type_code(t)])
+    for shape in [(7,), (0,), (33, 17), (4100, 3), (70_000, 2)]:
+        if dt.kind == "f":
+            a = (rng.uniform(0.999, 1.001, size=shape[::-1]) *
+                 np.where(rng.random(shape[::-1]) < 0.5, -1, 1)).astype(dt)
+        else:
+            a, _ = rand_array(rng, t, shape[::-1], -3, 3)
+        x = to_pdl(a, t)
+        got, exp = _run_both(op, [x])
+        rtol, atol, scale = _tol(op, a, exp, exp.type) if exp.type in FLOAT_TYPES else (0, 0, None)
+        assert_same(got, exp, rtol=rtol, atol=atol, scale=scale, what=f"{op} {t} {shape}")
+    a, _ = rand_array(rng, t, (9, 300), -3 if dt.kind != "f" else 0.9, 3 if dt.kind != "f" else 1.1,
+                      bad_frac=0.1)
+    x = to_pdl(a, t, badflag=True)
+    got, exp = _run_both(op, [x])
+    rtol, atol, scale = _tol(op, a, exp, exp.type) if exp.type in FLOAT_TYPES else (0, 0, None)
+    assert_same(got, exp, rtol=rtol, atol=atol, scale=scale, what=f"{op} {t} bad")
+    got, exp = _run_both(op, [to_pdl(a, t, badflag=True).xchg(0, 1)])
+    assert_same(got, exp, rtol=rtol, atol=atol, scale=scale if scale is None else None,
+                what=f"{op} {t} strided")
