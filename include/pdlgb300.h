@@ -176,6 +176,12 @@ pdlgb300_error pdlgb300_run_firstnonzeroover(pdlgb300_ndarray *a, pdlgb300_ndarr
  * is); dcumuprodover: double [o]b(n).                                     */
 pdlgb300_error pdlgb300_run_cumuprodover(pdlgb300_ndarray *a, pdlgb300_ndarray *b);
 pdlgb300_error pdlgb300_run_dcumuprodover(pdlgb300_ndarray *a, pdlgb300_ndarray *b);
+/* lib/PDL/Ufunc.pd:563-613  minmaximum: a(n); [o]cmin(); [o]cmax();
+ * indx [o]cmin_ind(); indx [o]cmax_ind() -- bad and NaN elements skipped,
+ * first index on ties; nothing left: all four BAD with their bad state.   */
+pdlgb300_error pdlgb300_run_minmaximum(pdlgb300_ndarray *a, pdlgb300_ndarray *cmin,
+                                       pdlgb300_ndarray *cmax, pdlgb300_ndarray *cmin_ind,
+                                       pdlgb300_ndarray *cmax_ind);
 /* lib/PDL/Ops.pd:104-153,288-289  plus/mult: a(); b(); [o]c(); int swap   */
 pdlgb300_error pdlgb300_run_plus(pdlgb300_ndarray *a, pdlgb300_ndarray *b,
                                  pdlgb300_ndarray *c, int swap);

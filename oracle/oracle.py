@@ -38,6 +38,8 @@ def lib() -> C.CDLL:
         L.oracle_redodims.restype = C.c_int
         L.oracle_redodims.argtypes = [C.c_char_p, A.PP, C.c_char_p, C.c_size_t]
         L.oracle_free.argtypes = [C.c_void_p]
+        L.oracle_npdls.restype = C.c_int
+        L.oracle_npdls.argtypes = [C.c_char_p]
         L.oracle_sumover_bwd.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_int64]
         L.oracle_average_bwd.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_int64]
         L.oracle_matmult_bwd.argtypes = [C.c_void_p] * 5 + [C.c_int64] * 6
@@ -57,6 +59,11 @@ def run(op: str, inputs, outputs=None, swap: int = 0, nthreads: int = 1):
     """Run `op` on the CPU oracle.  inputs: ndarrays; outputs: list of
     ndarray or None (null).  Returns the output ndarrays (host)."""
     outputs = outputs if outputs is not None else [None]
+    npdls = lib().oracle_npdls(op.encode())
+    if npdls < 0:
+        raise OracleError(f"unknown op {op}")
+    if len(inputs) + len(outputs) != npdls:
+        raise OracleError(f"{op} takes {npdls} ndarrays, got {len(inputs) + len(outputs)}")
     ds = [_host_desc(x) for x in inputs]
     keep = []
     for o in outputs:

@@ -41,7 +41,7 @@
 
 #include "../include/pdlgb300.h"
 
-#define MAXP 4
+#define MAXP 5
 #define MAXB (PDLGB300_MAXDIMS + 2)
 
 /* ------------------------------------------------------------------ types */
@@ -115,6 +115,7 @@ enum {
   OP_SHIFTRIGHT, OP_OR2, OP_AND2, OP_XOR,
   OP_ANDOVER, OP_OROVER, OP_XOROVER, OP_ZCOVER, OP_BANDOVER, OP_BOROVER,
   OP_BXOROVER, OP_FIRSTNONZEROOVER, OP_CUMUPRODOVER, OP_DCUMUPRODOVER,
+  OP_MINMAXIMUM,
   OP_N
 };
 #define IS_BIOP(op) ((op) == OP_PLUS || (op) == OP_MULT || ((op) >= OP_MINUS && (op) <= OP_XOR))
@@ -132,6 +133,7 @@ typedef struct {
   int out_typed;        /* 0, TYPED, TYPED|TPLUS for the output */
   int out_type;         /* typed output type */
   int int_only;         /* GenericTypes = the integer types (bit ops) */
+  int idx_from;         /* > 0: outputs from this parameter on are indx */
 } opdef;
 
 static const opdef OPS[OP_N] = {
@@ -177,6 +179,9 @@ static const opdef OPS[OP_N] = {
   {"firstnonzeroover", 2, 1, {"a", "b"}, {1, 0}, {{0}, {0}}, {"n"}, 0, -1},
   {"cumuprodover", 2, 1, {"a", "b"}, {1, 1}, {{0}, {0}}, {"n"}, TYPED | TPLUS, PDLGB300_L},
   {"dcumuprodover", 2, 1, {"a", "b"}, {1, 1}, {{0}, {0}}, {"n"}, TYPED, PDLGB300_D},
+  /* lib/PDL/Ufunc.pd:563-613 */
+  {"minmaximum", 5, 1, {"a", "cmin", "cmax", "cmin_ind", "cmax_ind"}, {1, 0, 0, 0, 0},
+   {{0}, {0}, {0}, {0}, {0}}, {"n"}, 0, -1, 0, 3},
 };
 
 static int find_op(const char *name) {
@@ -289,7 +294,7 @@ static int transtype_select(const opdef *op, pdlgb300_ndarray *const *pdls) {
   int ret = -1, use_last = 0;
   for (int i = op->npdls - 1; i >= 0; i--) {
     const pdlgb300_ndarray *p = pdls[i];
-    int is_typed = (i >= op->nparents) && op->out_typed;
+    int is_typed = (i >= op->nparents) && (op->out_typed || (op->idx_from && i >= op->idx_from));
     if (!(p->state & PDLGB300_NOMYDIMS) && !is_typed) {
       int t = p->datatype;
       int avail = t <= last;
@@ -302,7 +307,8 @@ static int transtype_select(const opdef *op, pdlgb300_ndarray *const *pdls) {
   return ret;
 }
 
-static int out_type_for(const opdef *op, int ttype) {
+static int out_type_for(const opdef *op, int ttype, int j) {
+  if (op->idx_from && j >= op->idx_from) return PDLGB300_IND;
   if (!op->out_typed) return ttype;
   if (op->out_typed & TPLUS) return op->out_type > ttype ? op->out_type : ttype;
   return op->out_type;
@@ -698,6 +704,48 @@ O_REAL_TYPES(DEF_AVGS)
   DEF_MM(maximum_ind_##SYM, CT, SYM, ISF, >, 1)
 O_REAL_TYPES(DEF_MMS)
 
+/* minmaximum: skip bad (bad mode) and NaN; strict < / > keep the first
+ * index; nothing left sets all four outputs bad (and their bad state) */
+#define DEF_MINMAXIMUM(NAME, T, SYM, ISF)                                                \
+  static void NAME(octx *c, const int64_t *offs, int64_t n0, const int64_t *inc0) { \
+    int64_t N = c->ind_sizes[0], ia = c->inc_sizes[0][0];                            \
+    T abad = c->bad[0].SYM;                                                          \
+    for (int64_t i0 = 0; i0 < n0; i0++) {                                            \
+      const T *a = (const T *)c->base[0] + offs[0] + i0 * inc0[0];                   \
+      T *cmin = (T *)c->base[1] + offs[1] + i0 * inc0[1];                            \
+      T *cmax = (T *)c->base[2] + offs[2] + i0 * inc0[2];                            \
+      int64_t *imin = (int64_t *)c->base[3] + offs[3] + i0 * inc0[3];                \
+      int64_t *imax = (int64_t *)c->base[4] + offs[4] + i0 * inc0[4];                \
+      T curmin = 0, curmax = 0;                                                      \
+      int64_t curmin_ind = 0, curmax_ind = 0;                                        \
+      int flag = 0;                                                                  \
+      for (int64_t n = 0; n < N; n++) {                                              \
+        T v = a[n * ia];                                                             \
+        if (c->bvalflag && ISBADV(v, abad, ISF)) continue;                           \
+        if (ISF && isnan((double)v)) continue;                                       \
+        if (!flag) {                                                                 \
+          curmin = curmax = v;                                                       \
+          curmin_ind = curmax_ind = n;                                               \
+          flag = 1;                                                                  \
+        } else {                                                                     \
+          if (v < curmin) { curmin = v; curmin_ind = n; }                            \
+          if (v > curmax) { curmax = v; curmax_ind = n; }                            \
+        }                                                                            \
+      }                                                                              \
+      if (!flag) {                                                                   \
+        *cmin = c->bad[1].SYM;                                                       \
+        *cmax = c->bad[2].SYM;                                                       \
+        *imin = c->bad[3].N;                                                         \
+        *imax = c->bad[4].N;                                                         \
+        c->setbad_out = 1;                                                           \
+      } else {                                                                       \
+        *cmin = curmin; *cmax = curmax; *imin = curmin_ind; *imax = curmax_ind;      \
+      }                                                                              \
+    }                                                                                \
+  }
+#define DEF_MINMAXIMUMS(E, CT, SYM, IP, ISF, UNS) DEF_MINMAXIMUM(minmaximum_##SYM, CT, SYM, ISF)
+O_REAL_TYPES(DEF_MINMAXIMUMS)
+
 /* plus/mult: a(); b(); [o]c() */
 #define DEF_BIOP(NAME, T, SYM, ISF, OP)                                                 \
   static void NAME(octx *c, const int64_t *offs, int64_t n0, const int64_t *inc0) { \
@@ -903,6 +951,7 @@ static body_fn pick_body(int op, int t) {
     CASE(OP_FIRSTNONZEROOVER, firstnonzeroover)
     CASE(OP_CUMUPRODOVER, cumuprodover)
     CASE(OP_DCUMUPRODOVER, dcumuprodover)
+    CASE(OP_MINMAXIMUM, minmaximum)
   }
 #undef CASE
   return NULL;
@@ -998,7 +1047,7 @@ int oracle_redodims(const char *opname, pdlgb300_ndarray **pdls, char *msg,
   if (do_redodims(&e, d, pdls, &b)) return 1;
   for (int j = d->nparents; j < d->npdls; j++)
     if (pdls[j]->state & PDLGB300_NOMYDIMS) {
-      pdls[j]->datatype = out_type_for(d, tt);
+      pdls[j]->datatype = out_type_for(d, tt, j);
       pdls[j]->state &= ~PDLGB300_NOMYDIMS;
     }
   return 0;
@@ -1010,6 +1059,13 @@ int oracle_redodims(const char *opname, pdlgb300_ndarray **pdls, char *msg,
  * nthreads <= 1 runs single-threaded; otherwise the reference's
  * auto-pthread split (only when some pdl has >= 2^20 elements, the default
  * PDL_AUTOPTHREAD_SIZE of 1 Mi elements). */
+/* Number of ndarray arguments (parents + children) of an op, -1 if unknown:
+   callers size the argument array with it. */
+int oracle_npdls(const char *opname) {
+  int op = find_op(opname);
+  return op < 0 ? -1 : OPS[op].npdls;
+}
+
 int oracle_run(const char *opname, pdlgb300_ndarray **pdls_in, const int64_t *other,
                int nthreads, char *msg, size_t msglen) {
   errbuf e = {msg, msglen};
@@ -1042,7 +1098,7 @@ int oracle_run(const char *opname, pdlgb300_ndarray **pdls_in, const int64_t *ot
   void *tofree[MAXP] = {0};
   for (int j = 0; j < d->npdls; j++) {
     pdlgb300_ndarray *p = pdls[j];
-    int want = j < d->nparents ? tt : out_type_for(d, tt);
+    int want = j < d->nparents ? tt : out_type_for(d, tt, j);
     if (creating[j]) {
       int64_t n = 1;
       for (int i = 0; i < p->ndims; i++) n *= p->dims[i];

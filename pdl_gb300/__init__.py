@@ -18,7 +18,7 @@ from .ndarray import (  # noqa: F401
 from .ndarray import (  # noqa: F401
     and2, divide, eq, ge, gt, le, lt, minus, ne, or2, shiftleft, shiftright, xor, xor2,
     andover, bandover, borover, bxorover, firstnonzeroover, orover, xorover, zcover,
-    cumuprodover, dcumuprodover)
+    cumuprodover, dcumuprodover, minmaximum, minmaxover)
 from ._abi import MATMULT_BF16X3, MATMULT_BF16X6, MATMULT_SIMT_EXACT, MATMULT_SIMT_FP32  # noqa: F401
 
 __all__ = [n for n in dir() if not n.startswith("_")]

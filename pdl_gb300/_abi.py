@@ -94,6 +94,7 @@ SIGNATURES = {
     "pdlgb300_run_minimum": (Error, [P, P]),
     "pdlgb300_run_maximum": (Error, [P, P]),
     "pdlgb300_run_minimum_ind": (Error, [P, P]),
+    "pdlgb300_run_minmaximum": (Error, [P, P, P, P, P]),
     **{f"pdlgb300_run_{op}": (Error, [P, P])
        for op in ("andover", "orover", "xorover", "zcover", "bandover", "borover",
                   "bxorover", "firstnonzeroover", "cumuprodover", "dcumuprodover")},

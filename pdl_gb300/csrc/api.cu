@@ -118,7 +118,7 @@ enum OpId {
   O_MINUS, O_DIVIDE, O_GT, O_LT, O_LE, O_GE, O_EQ, O_NE,
   O_SHIFTLEFT, O_SHIFTRIGHT, O_OR2, O_AND2, O_XOR,
   O_ANDOVER, O_OROVER, O_XOROVER, O_ZCOVER, O_BANDOVER, O_BOROVER, O_BXOROVER,
-  O_FIRSTNONZEROOVER, O_CUMUPRODOVER, O_DCUMUPRODOVER, O_NOPS
+  O_FIRSTNONZEROOVER, O_CUMUPRODOVER, O_DCUMUPRODOVER, O_MINMAXIMUM, O_NOPS
 };
 
 // binary ops (a(); b(); [o]c(); int swap) and their kernel codes
@@ -151,6 +151,7 @@ const char *const N_AC[] = {"a", "c"};
 const char *const N_ABC[] = {"a", "b", "c"};
 const char *const N_ABDC[] = {"a", "b", "d", "c"};
 const char *const I_N[] = {"n"};
+const char *const N_MM4[] = {"a", "cmin", "cmax", "cmin_ind", "cmax_ind"};
 const char *const I_THW[] = {"t", "h", "w"};
 
 const int32_t RD_10[] = {1, 0}, RD_11[] = {1, 1}, RD_000[] = {0, 0, 0},
@@ -160,6 +161,8 @@ const int32_t F_TP[] = {0, OUT_TP}, F_T[] = {0, OUT_T}, F_C[] = {0, OUT_C},
 const int32_t PT_L[] = {-1, PDLGB300_L}, PT_D[] = {-1, PDLGB300_D},
               PT_N[] = {-1, PDLGB300_IND}, PT_NONE[] = {-1, -1, -1, -1},
               PT_SMP[] = {-1, -1, -1, PDLGB300_L};
+const int32_t RD_10000[] = {1, 0, 0, 0, 0}, F_MM4[] = {0, OUT_C, OUT_C, OUT_T, OUT_T},
+              PT_MM4[] = {-1, -1, -1, PDLGB300_IND, PDLGB300_IND};
 const int32_t ID_N0[] = {0}, ID_NN[] = {0, 0}, ID_NNN[] = {0, 0, 0},
               ID_MM[] = {0, 1, 2, 0, 2, 1}, ID_NONE[] = {0};
 
@@ -206,6 +209,8 @@ const pdlgb300_vtable VT[O_NOPS] = {
     // lib/PDL/Ufunc.pd:120-140 with `*=`: a(n); int+ [o]b(n) / double [o]b(n)
     {"cumuprodover", 2, 1, 1, 0, N_AB, RD_11, F_TP, PT_L, ID_NN, I_N, GENTYPES},
     {"dcumuprodover", 2, 1, 1, 0, N_AB, RD_11, F_T, PT_D, ID_NN, I_N, REALTYPES},
+    // lib/PDL/Ufunc.pd:563-613
+    {"minmaximum", 5, 1, 1, 0, N_MM4, RD_10000, F_MM4, PT_MM4, ID_N0, I_N, REALTYPES},
 };
 
 int op_of(const pdlgb300_vtable *vt) {
@@ -844,6 +849,7 @@ pdlgb300_error run_impl(const pdlgb300_vtable *vt, pdlgb300_ndarray *const *pdls
   const bool minmax = op == O_MINIMUM || op == O_MAXIMUM || op == O_MINIMUM_IND ||
                       op == O_MAXIMUM_IND;
   const bool need_flag = (minmax && (c.bvalflag || c.b.ind_sizes[0] == 0)) ||
+                         op == O_MINMAXIMUM ||  // an all-NaN row sets bad without bad mode
                          ((is_biop(op) || op == O_INNER) && c.bvalflag);
   if (!e.error) e = setbad_word(&c.d_setbad);
   if (!e.error && need_flag) {
@@ -1122,6 +1128,29 @@ pdlgb300_error dispatch_cumusum(RunCtx &c, int dop) {
   return e;
 }
 
+pdlgb300_error dispatch_minmaximum(RunCtx &c) {
+  MM4Args g;
+  memset(&g, 0, sizeof g);
+  const int which[5] = {0, 1, 2, 3, 4};
+  g.L = collapse(c.b, 5, which);
+  g.rows = g.L.total;
+  g.n = c.b.ind_sizes[0];
+  g.inc_n = g.n <= 1 ? 1 : c.b.inc_sizes[0][0];
+  g.a = c.dev[0];
+  for (int i = 0; i < 4; i++) {
+    g.out[i] = c.dev[1 + i];
+    g.obad[i] = bad_bits(&c.v[1 + i]);
+  }
+  g.bad = c.bvalflag;
+  g.abad = bad_bits(&c.v[0]);
+  g.abad_isnan = bad_isnan(&c.v[0]);
+  g.setbad = c.d_setbad;
+  tl_info.rows = g.rows;
+  tl_info.n = g.n;
+  tl_info.bytes = (double)g.rows * g.n * TSIZES[c.v[0].datatype];
+  return launch_minmaximum(c.v[0].datatype, g, g_stream);
+}
+
 pdlgb300_error dispatch_biop(RunCtx &c, int which_op) {
   BiopArgs g;
   memset(&g, 0, sizeof g);
@@ -1307,6 +1336,7 @@ pdlgb300_error dispatch(RunCtx &c, const int64_t *) {
     case O_BOROVER: return dispatch_reduce(c, R_BOR);
     case O_BXOROVER: return dispatch_reduce(c, R_BXOR);
     case O_FIRSTNONZEROOVER: return dispatch_reduce(c, R_FIRSTNZ);
+    case O_MINMAXIMUM: return dispatch_minmaximum(c);
     case O_CUMUPRODOVER: return dispatch_cumusum(c, 2);
     case O_DCUMUPRODOVER: return dispatch_cumusum(c, 3);
     case O_INNER: return dispatch_inner(c);
@@ -1445,6 +1475,13 @@ RUN2(bxorover, O_BXOROVER)
 RUN2(firstnonzeroover, O_FIRSTNONZEROOVER)
 RUN2(cumuprodover, O_CUMUPRODOVER)
 RUN2(dcumuprodover, O_DCUMUPRODOVER)
+
+pdlgb300_error pdlgb300_run_minmaximum(pdlgb300_ndarray *a, pdlgb300_ndarray *cmin,
+                                       pdlgb300_ndarray *cmax, pdlgb300_ndarray *cmin_ind,
+                                       pdlgb300_ndarray *cmax_ind) {
+  pdlgb300_ndarray *p[5] = {a, cmin, cmax, cmin_ind, cmax_ind};
+  return guard_run(O_MINMAXIMUM, p, nullptr);
+}
 
 pdlgb300_error pdlgb300_run_plus(pdlgb300_ndarray *a, pdlgb300_ndarray *b, pdlgb300_ndarray *c,
                                  int swap) {

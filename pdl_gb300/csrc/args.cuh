@@ -72,6 +72,20 @@ struct BiopArgs {
 };
 pdlgb300_error launch_biop(int op, int dt, const BiopArgs &g, cudaStream_t s);
 
+// minmaximum: a(n) -> cmin, cmax, cmin_ind, cmax_ind (pdls 1..4 of L)
+struct MM4Args {
+  const char *a;
+  char *out[4];
+  int64_t n, inc_n, rows;
+  Loop L;  // pdl 0 a, 1 cmin, 2 cmax, 3 cmin_ind, 4 cmax_ind
+  int bad;
+  uint64_t abad;
+  int abad_isnan;
+  uint64_t obad[4];
+  int *setbad;
+};
+pdlgb300_error launch_minmaximum(int dt, const MM4Args &g, cudaStream_t s);
+
 struct ConvArgs {
   const char *src;
   char *dst;

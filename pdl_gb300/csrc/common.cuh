@@ -13,7 +13,7 @@
 
 namespace pg {
 
-constexpr int MAXP = 4;                       // max ndarrays of one op
+constexpr int MAXP = 5;                       // max ndarrays of one op (minmaximum: 5)
 constexpr int MAXB = PDLGB300_MAXDIMS + 2;    // max broadcast dims
 constexpr int NSM_GB300 = 152;
 

@@ -473,6 +473,17 @@ borover = _red("borover")
 bxorover = _red("bxorover")
 firstnonzeroover = _red("firstnonzeroover")
 cumuprodover = _red("cumuprodover")
+
+
+def minmaximum(a, cmin=None, cmax=None, cmin_ind=None, cmax_ind=None):
+    """(cmin, cmax, cmin_ind, cmax_ind) over dim 0 (lib/PDL/Ufunc.pd:563-613;
+    alias minmaxover)."""
+    a = _scalar_to_pdl(a, None)
+    outs = [None if o is None or isinstance(o, _Null) else o for o in (cmin, cmax, cmin_ind, cmax_ind)]
+    return tuple(_run("minmaximum", [a], outs))
+
+
+minmaxover = minmaximum
 dcumuprodover = _red("dcumuprodover")
 minimum_ind = _red("minimum_ind")
 maximum_ind = _red("maximum_ind")

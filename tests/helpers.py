@@ -3,6 +3,7 @@ same data, and comparing with the tolerances the parity bar states."""
 from __future__ import annotations
 
 import json
+import zlib
 from pathlib import Path
 
 import numpy as np
@@ -66,6 +67,11 @@ def expect_array(case, like_type=None):
 
 
 def seeded(seed):
+    """A generator from an int or from a tuple of strings/ints; tuples are
+    hashed with CRC-32 so the seed is the same in every process (Python's
+    str hash is salted per process)."""
+    if isinstance(seed, tuple):
+        seed = zlib.crc32(repr(seed).encode())
     return np.random.default_rng(seed)
 
 

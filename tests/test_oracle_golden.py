@@ -40,7 +40,8 @@ def run_case_oracle(case):
         out = (P.zeroes if kind == "zeroes" else P.ones)("double", *dims)
     if case["op"] == "matmult":
         return oracle_matmult(ins[0], ins[1], out)
-    return O.run(case["op"], ins, [out], swap=case.get("swap", 0))[0]
+    outs = [out] + [None] * (case.get("nout", 1) - 1)
+    return O.run(case["op"], ins, outs, swap=case.get("swap", 0))[case.get("pick", 0)]
 
 
 def check_result(case, got):
