@@ -19,6 +19,9 @@ from .ndarray import (  # noqa: F401
     and2, divide, eq, ge, gt, le, lt, minus, ne, or2, shiftleft, shiftright, xor, xor2,
     andover, bandover, borover, bxorover, firstnonzeroover, orover, xorover, zcover,
     cumuprodover, dcumuprodover, minmaximum, minmaxover)
+from .whole import (  # noqa: F401
+    all, and_, any, avg, band, bor, bxor, davg, dprod, dsum, max, min, or_, prod, sum,
+    xorall, zcheck)
 from ._abi import MATMULT_BF16X3, MATMULT_BF16X6, MATMULT_SIMT_EXACT, MATMULT_SIMT_FP32  # noqa: F401
 
 __all__ = [n for n in dir() if not n.startswith("_")]

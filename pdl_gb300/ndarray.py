@@ -200,6 +200,78 @@ class ndarray:
         s.insert(pos, 0)
         return self._view(d, s, self.offs)
 
+    def mv(self, n1: int, n2: int) -> "ndarray":
+        """Move dim n1 to position n2, the dims between shifting over
+        (lib/PDL/Slices.pd:1563-1587; negative dims count from the end)."""
+        nd = self.ndims
+        a, b = n1 + nd if n1 < 0 else n1, n2 + nd if n2 < 0 else n2
+        if min(a, b) < 0 or max(a, b) >= nd:
+            raise PDLError(A.EUSERERROR, f"One of dims {n1}, {n2} out of range: should be 0<=dim<{nd}")
+        d, s = list(self.dims), list(self.incs)
+        d.insert(b, d.pop(a))
+        s.insert(b, s.pop(a))
+        return self._view(d, s, self.offs)
+
+    def clump(self, *args) -> "ndarray":
+        """Merge dims into one (lib/PDL/Core.pm:1806-1864, Slices.pd:1373-1398).
+        clump(n): n > 0 the first n dims, -1 all of them, n < -1 leaves -n-1
+        dims behind; clump(d1, d2, ...): those dims, merged in the order given
+        and placed at the lowest of them.  The result is a view when the
+        merged dims have compatible strides, else a contiguous copy made on
+        the ndarray's side (host or device), into which assignments do not
+        flow back."""
+        if len(args) > 1:
+            nd = self.ndims
+            if len(args) > nd:
+                raise PDLError(A.EUSERERROR, "too many dimensions")
+            seen = set()
+            for k in args:
+                if k > nd - 1:
+                    raise PDLError(A.EUSERERROR, f"dimension index {k} larger than greatest dimension")
+                if k in seen:
+                    raise PDLError(A.EUSERERROR, f"duplicate dimension {k}")
+                seen.add(k)
+            order = list(args) + [k for k in range(nd) if k not in seen]
+            v = self._view([self.dims[k] for k in order], [self.incs[k] for k in order], self.offs)
+            v = v.clump(len(args))
+            targd = min(min(args), nd - 1)
+            return v.mv(0, targd) if targd > 0 else v
+        n = int(args[0])
+        nd = self.ndims
+        if n > nd:
+            n = nd
+        if n < -1:
+            n = max(nd + n + 1, 0)
+        nrem = nd if n == -1 else n
+        d1 = int(np.prod(self.dims[:nrem], dtype=np.int64)) if nrem else 1
+        rest_d, rest_s = list(self.dims[nrem:]), list(self.incs[nrem:])
+        inc, ok = None, True
+        for k in range(nrem):
+            if self.dims[k] == 1:
+                continue
+            if inc is None:
+                inc = self.incs[k]
+            elif self.incs[k] != expect:
+                ok = False
+                break
+            expect = self.incs[k] * self.dims[k]
+        if d1 == 0:
+            ok, inc = True, 1
+        if ok:
+            return self._view([d1] + rest_d, [1 if inc is None else inc] + rest_s, self.offs)
+        c = convert(self, self.datatype)
+        c._badvalue = self._badvalue
+        c._badflag = self._badflag
+        return c.clump(n)
+
+    def flat(self) -> "ndarray":
+        """clump(-1) unless already 1-D (lib/PDL/Core.pm:3071-3073)."""
+        return self if self.ndims == 1 else self.clump(-1)
+
+    def sclr(self):
+        """The first element as a Python number."""
+        return self.numpy().reshape(-1)[0].item()
+
     def slice(self, *specs) -> "ndarray":
         """Per dim: slice(start, stop, step) or an int (drops the dim)."""
         d, s, o = [], [], self.offs
@@ -281,6 +353,27 @@ class ndarray:
     def minimum_ind(self, out=None): return minimum_ind(self, out)
     def maximum_ind(self, out=None): return maximum_ind(self, out)
     def inner(self, o, out=None): return inner(self, o, out)
+    def minmaximum(self): return minmaximum(self)
+
+    # whole-array reductions (lib/PDL/Ufunc.pd:615-663): flat, then the
+    # reduction over dim 0
+    def sum(self): return self.flat().sumover()
+    def avg(self): return self.flat().average()
+    def prod(self): return self.flat().prodover()
+    def dsum(self): return self.flat().dsumover()
+    def davg(self): return self.flat().daverage()
+    def dprod(self): return self.flat().dprodover()
+    def zcheck(self): return zcover(self.flat())
+    def and_(self): return andover(self.flat())
+    def band(self): return bandover(self.flat())
+    def or_(self): return orover(self.flat())
+    def bor(self): return borover(self.flat())
+    def xorall(self): return xorover(self.flat())
+    def bxor(self): return bxorover(self.flat())
+    def min(self): return self.flat().minimum()
+    def max(self): return self.flat().maximum()
+    any = or_
+    all = and_
     def matmult(self, o, out=None): return matmult(self, o, out)
 
 

@@ -481,6 +481,10 @@ def _golden_gpu(case):
     ins = [make_input(s) for s in case["inputs"]]
     if case.get("view") == "xchg01":
         ins[0] = ins[0].xchg(0, 1)
+    if case.get("view") == "dim1_index1":
+        ins[0] = ins[0].slice(slice(None), 1)
+    if "whole" in case:
+        return getattr(P, case["whole"])(ins[0])
     out = None
     if "out" in case:
         kind, dims = case["out"].split(":")
@@ -685,3 +689,45 @@ def test_minmaximum_doc_example(gpu):
     assert cmin.numpy().tolist() == [-2, 0] and cmax.numpy().tolist() == [4, 3]
     assert imin.numpy().tolist() == [0, 1] and imax.numpy().tolist() == [2, 2]
     assert not cmin.badflag() and imin.type == "indx"
+
+
+WHOLE = [("sum", "sumover"), ("avg", "average"), ("prod", "prodover"), ("dsum", "dsumover"),
+         ("davg", "daverage"), ("dprod", "dprodover"), ("zcheck", "zcover"), ("and_", "andover"),
+         ("band", "bandover"), ("or_", "orover"), ("bor", "borover"), ("xorall", "xorover"),
+         ("bxor", "bxorover"), ("min", "minimum"), ("max", "maximum")]
+
+
+@pytest.mark.parametrize("t", ["byte", "long", "longlong", "float", "double"])
+def test_whole_array_reductions(gpu, t):
+    """Ufunc.pd:615-663: each whole-array function is flat then the
+    reduction over dim 0; against the oracle on the flattened ndarray,
+    including a view whose dims do not merge (flat makes a device copy) and
+    bad values.  Sums and products of floats within the sequential bound."""
+    rng = seeded(("whole", t))
+    a, _ = rand_array(rng, t, (6, 5, 7), -3, 3)
+    x = to_pdl(a, t)
+    ab, _ = rand_array(rng, t, (40, 50), -3, 3, bad_frac=0.2)
+    xb = to_pdl(ab, t, badflag=True)
+    for name, op in WHOLE:
+        if op in ("bandover", "borover", "bxorover") and t in ("float", "double"):
+            cases = [(x, x.flat())]
+        else:
+            cases = [(x, x.flat()), (xb, xb.flat())]
+        # a strided view: dims (7, 6) of the (7, 5, 6) ndarray at index 2 of dim 1
+        v = x.slice(slice(None), 2)
+        cases.append((v, P.pdl(np.ascontiguousarray(v.numpy()))))
+        cases.append((x.xchg(0, 2), P.pdl(np.ascontiguousarray(x.xchg(0, 2).numpy()))))
+        for src, flat in cases:
+            got = getattr(P, name)(src.to_device() if src is x else src)
+            exp = O.run(op, [flat.flat()])[0]
+            assert got.dims == () and exp.dims == ()
+            if op in ("prodover", "dprodover") and t in ("float", "double"):
+                n = flat.nelem
+                assert_same(got, exp, rtol=(n + 2) * EPS[t], atol=1e-300, what=f"{name} {t}")
+            elif op in ("sumover", "average", "dsumover", "daverage") and t in ("float", "double"):
+                n = flat.nelem
+                absum = np.abs(flat.numpy().astype(np.float64)).sum()
+                eps = EPS["double"] if op.startswith("d") else EPS[t]
+                assert_same(got, exp, atol=(n + 2) * eps * absum, what=f"{name} {t}")
+            else:
+                assert_same(got, exp, what=f"{name} {t}")

@@ -33,6 +33,10 @@ def run_case_oracle(case):
     ins = [make_input(s) for s in case["inputs"]]
     if case.get("view") == "xchg01":
         ins[0] = ins[0].xchg(0, 1)
+    if case.get("view") == "dim1_index1":
+        ins[0] = ins[0].slice(slice(None), 1)
+    if "whole" in case:
+        ins[0] = ins[0].flat()
     out = None
     if "out" in case:
         kind, dims = case["out"].split(":")
