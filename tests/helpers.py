@@ -130,8 +130,10 @@ def assert_same(got: P.ndarray, exp: P.ndarray, rtol=0.0, atol=0.0, scale=None, 
     if scale is None:
         scale = np.abs(e)
     scale = np.broadcast_to(scale, e.shape)
-    diff = np.abs(g.astype(np.float64) - e.astype(np.float64))
+    with np.errstate(invalid="ignore"):
+        diff = np.abs(g.astype(np.float64) - e.astype(np.float64))
     tol = atol + rtol * np.abs(scale)
-    bad = m & ~(diff <= tol)
+    # equal infinities differ by NaN: equality passes before the tolerance
+    bad = m & ~((g == e) | (diff <= tol))
     assert not bad.any(), (f"{what}: {bad.sum()} values outside tolerance; worst diff "
                            f"{diff[m].max() if m.any() else 0} tol {tol[bad].ravel()[:4]}")
