@@ -182,6 +182,22 @@ pdlgb300_error pdlgb300_run_dcumuprodover(pdlgb300_ndarray *a, pdlgb300_ndarray 
 pdlgb300_error pdlgb300_run_minmaximum(pdlgb300_ndarray *a, pdlgb300_ndarray *cmin,
                                        pdlgb300_ndarray *cmax, pdlgb300_ndarray *cmin_ind,
                                        pdlgb300_ndarray *cmax_ind);
+/* A deferred expression of PDL::Ops binary ops (lib/PDL/Ops.pd:104-153,
+ * 288-307) reduced over dim 0 by a PDL::Ufunc reduction in one pass, with
+ * the result the ops and the reduction give one after the other
+ * (lib/PDL/Ufunc.pd:94-187, 413-500).  No reference function is replaced:
+ * the reference always materialises each op (the broadcast loop of
+ * lib/PDL/Core/pdlbroadcast.c runs once per op).  Node k applies `op` (a
+ * binary-op vtable) to operands a, b: 0..nleaf-1 the leaves, nleaf+j node
+ * j < k; the last node is the expression.  Leaves share one type (int32,
+ * int64, float or double); `out` null or of the reduction's output type.  */
+typedef struct {
+  const pdlgb300_vtable *op;
+  int32_t a, b;
+} pdlgb300_expr_node;
+pdlgb300_error pdlgb300_run_expr_reduce(const pdlgb300_vtable *reduction, int32_t nleaf,
+                                        pdlgb300_ndarray *const *leaves, int32_t nnode,
+                                        const pdlgb300_expr_node *nodes, pdlgb300_ndarray *out);
 /* lib/PDL/Ops.pd:104-153,288-289  plus/mult: a(); b(); [o]c(); int swap   */
 pdlgb300_error pdlgb300_run_plus(pdlgb300_ndarray *a, pdlgb300_ndarray *b,
                                  pdlgb300_ndarray *c, int swap);

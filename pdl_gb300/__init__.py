@@ -22,6 +22,7 @@ from .ndarray import (  # noqa: F401
 from .whole import (  # noqa: F401
     all, and_, any, avg, band, bor, bxor, davg, dprod, dsum, max, min, or_, prod, sum,
     xorall, zcheck)
+from .lazy import Lazy, lazy  # noqa: F401
 from ._abi import MATMULT_BF16X3, MATMULT_BF16X6, MATMULT_SIMT_EXACT, MATMULT_SIMT_FP32  # noqa: F401
 
 __all__ = [n for n in dir() if not n.startswith("_")]

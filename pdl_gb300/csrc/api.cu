@@ -21,7 +21,7 @@
 #include <string>
 #include <vector>
 
-#include "args.cuh"
+#include "biop.cuh"
 
 // ================================================================ helpers
 namespace {
@@ -1354,6 +1354,268 @@ pdlgb300_error guard_run(int op, pdlgb300_ndarray *const *pdls, const int64_t *o
   }
 }
 
+// ------------------------------------------------------ fused expressions
+
+int redop_of(int op) {
+  switch (op) {
+    case O_SUMOVER: return R_SUM;
+    case O_DSUMOVER: return R_DSUM;
+    case O_PRODOVER: return R_PROD;
+    case O_DPRODOVER: return R_DPROD;
+    case O_AVERAGE: return R_AVG;
+    case O_DAVERAGE: return R_DAVG;
+    case O_MINIMUM: return R_MIN;
+    case O_MAXIMUM: return R_MAX;
+    case O_MINIMUM_IND: return R_MIN_IND;
+    case O_MAXIMUM_IND: return R_MAX_IND;
+    case O_ANDOVER: return R_AND;
+    case O_OROVER: return R_OR;
+    case O_XOROVER: return R_XOR;
+    case O_ZCOVER: return R_ZC;
+    case O_BANDOVER: return R_BAND;
+    case O_BOROVER: return R_BOR;
+    case O_BXOROVER: return R_BXOR;
+    case O_FIRSTNONZEROOVER: return R_FIRSTNZ;
+    default: return -1;
+  }
+}
+
+// The expression's value is what the ops would materialise one by one; its
+// dims are the broadcast of the leaves' dims (size-1 dims stretch), its bad
+// flag the OR of the leaves' flags.  The reduction then runs on it as on a
+// materialised ndarray: same type selection, output shape and bad rules.
+pdlgb300_error run_expr_impl(const pdlgb300_vtable *rvt, int nleaf,
+                             pdlgb300_ndarray *const *leaves, int nnode,
+                             const pdlgb300_expr_node *nodes, pdlgb300_ndarray *out) {
+  const int rop = op_of(rvt);
+  const int redop = rop < 0 ? -1 : redop_of(rop);
+  if (redop < 0) return err(PDLGB300_EUSERERROR, "expression reduction: not a reduction over dim 0");
+  if (nleaf < 1 || nleaf > EXPR_MAXL || nnode < 1 || nnode > EXPR_MAXN)
+    return err(PDLGB300_EUSERERROR, "expression reduction: %d leaves and %d ops (at most %d and %d)",
+               nleaf, nnode, EXPR_MAXL, EXPR_MAXN);
+  if (!out) return err(PDLGB300_EUSERERROR, "%s: output is NULL", rvt->name);
+  keep_pool_cached();
+  memset(&tl_info, 0, sizeof tl_info);
+  snprintf(tl_info.op, sizeof tl_info.op, "%s(expr)", rvt->name);
+  const int T = leaves[0] ? leaves[0]->datatype : -1;
+  int lflag[EXPR_MAXL] = {0}, nflag[EXPR_MAXN] = {0};
+  int nd = 0;
+  for (int l = 0; l < nleaf; l++) {
+    const pdlgb300_ndarray *x = leaves[l];
+    if (!x || (x->state & PDLGB300_NOMYDIMS))
+      return err(PDLGB300_EUSERERROR, "expression reduction: leaf %d is null", l);
+    if (x->datatype != T)
+      return err(PDLGB300_EUSERERROR, "expression reduction: leaves of types %s and %s", TNAMES[T],
+                 TNAMES[x->datatype]);
+    if (x->ndims < 0 || x->ndims > PDLGB300_MAXDIMS)
+      return err(PDLGB300_EUSERERROR, "expression reduction: leaf %d has %d dims", l, x->ndims);
+    lflag[l] = !!(x->state & PDLGB300_BADVAL);
+    nd = std::max(nd, x->ndims);
+  }
+  if (!expr_fusable(redop, T))
+    return err(PDLGB300_EUSERERROR, "expression reduction: %s over %s is not fused", rvt->name,
+               T >= 0 && T < PDLGB300_NTYPES ? TNAMES[T] : "?");
+  const bool is_int = T < PDLGB300_F;
+  ExprArgs g;
+  memset(&g, 0, sizeof g);
+  std::vector<bool> used(nleaf + nnode, false);
+  for (int k = 0; k < nnode; k++) {
+    const pdlgb300_expr_node &q = nodes[k];
+    const int op = q.op ? op_of(q.op) : -1;
+    if (op < 0 || !is_biop(op))
+      return err(PDLGB300_EUSERERROR, "expression reduction: op %d is not a binary op of PDL::Ops", k);
+    const int code = biop_code_of(op);
+    if (!is_int && code >= B_SHL)
+      return err(PDLGB300_EUSERERROR, "expression reduction: %s works in an integer type", q.op->name);
+    int ab[2] = {q.a, q.b};
+    for (int i = 0; i < 2; i++) {
+      if (ab[i] < 0 || ab[i] >= nleaf + k)
+        return err(PDLGB300_EUSERERROR, "expression reduction: op %d operand %d refers to %d", k, i, ab[i]);
+      used[ab[i]] = true;
+      nflag[k] |= ab[i] < nleaf ? lflag[ab[i]] : nflag[ab[i] - nleaf];
+      ab[i] = ab[i] < nleaf ? ab[i] : EXPR_MAXL + (ab[i] - nleaf);
+    }
+    g.node[k] = ExprNode{code, ab[0], ab[1]};
+  }
+  for (int i = 0; i < nleaf + nnode - 1; i++)
+    if (!used[i])
+      return err(PDLGB300_EUSERERROR, "expression reduction: %s %d does not reach the result",
+                 i < nleaf ? "leaf" : "op", i < nleaf ? i : i - nleaf);
+  // the expression's dims
+  int64_t E[PDLGB300_MAXDIMS];
+  for (int k = 0; k < nd; k++) {
+    E[k] = 1;
+    for (int l = 0; l < nleaf; l++) {
+      const int64_t d = k < leaves[l]->ndims ? leaves[l]->dims[k] : 1;
+      if (d == 1) continue;
+      if (E[k] == 1) E[k] = d;
+      else if (E[k] != d)
+        return err(PDLGB300_EUSERERROR,
+                   "expression reduction: mismatched broadcast dimension %d: size %lld vs. %lld", k,
+                   (long long)E[k], (long long)d);
+    }
+  }
+  const int rootflag = nflag[nnode - 1];
+  pdlgb300_ndarray root;
+  memset(&root, 0, sizeof root);
+  root.datatype = T;
+  root.ndims = nd;
+  for (int k = 0; k < nd; k++) root.dims[k] = E[k];
+  default_incs(&root);
+  root.state = rootflag ? PDLGB300_BADVAL : 0;
+  root.badvalue.type = -1;
+  pdlgb300_ndarray *rp[2] = {&root, out};
+  const int tt = transtype_select(rvt, rp);
+  const int otype = out_type(rvt, 1, tt);
+  if (tt != T)
+    return err(PDLGB300_EUSERERROR, "expression reduction: %s would convert %s to %s", rvt->name,
+               TNAMES[T], TNAMES[tt]);
+  const bool creating = out->state & PDLGB300_NOMYDIMS;
+  if (creating) {
+    out->datatype = otype;
+    out->has_badvalue = 0;
+    out->badvalue.type = -1;
+  } else if (out->datatype != otype) {
+    return err(PDLGB300_EUSERERROR, "expression reduction: output type %s, %s gives %s",
+               TNAMES[out->datatype], rvt->name, TNAMES[otype]);
+  }
+  Brc rb;
+  RET_IF(plan_broadcast(rvt, rp, rb));
+  if (creating) {
+    out->state &= ~PDLGB300_NOMYDIMS;
+    if (!out->data && !out->ddata) {
+      void *d = nullptr;
+      RET_IF(dalloc((size_t)std::max<int64_t>(nvals(out), 1) * TSIZES[out->datatype], &d));
+      out->ddata = d;
+    }
+  }
+  // the kernel's loop: broadcast dims 1.. of the expression, leaves 0..3,
+  // the output at EXPR_MAXL
+  const int64_t n = nd > 0 ? E[0] : 1;
+  Brc b;
+  b.np = EXPR_MAXL + 1;
+  b.ndims = std::max(nd - 1, 1);
+  for (int k = 0; k < MAXB; k++) {
+    b.dims[k] = 1;
+    for (int p = 0; p < MAXP; p++) b.incs[k][p] = 0;
+  }
+  for (int k = 0; k + 1 < nd; k++) {
+    b.dims[k] = E[k + 1];
+    for (int l = 0; l < nleaf; l++)
+      if (k + 1 < leaves[l]->ndims && leaves[l]->dims[k + 1] == E[k + 1])
+        b.incs[k][l] = leaves[l]->incs[k + 1];
+    b.incs[k][EXPR_MAXL] = k < out->ndims ? out->incs[k] : 0;
+  }
+  Operand opd[EXPR_MAXL + 1];
+  pdlgb300_error e = ok();
+  for (int l = 0; l < nleaf && !e.error; l++) e = stage(leaves[l], false, opd[l]);
+  if (!e.error) e = stage(out, true, opd[EXPR_MAXL]);
+  const int which[EXPR_MAXL + 1] = {0, 1, 2, 3, EXPR_MAXL};
+  g.L = collapse(b, EXPR_MAXL + 1, which);
+  g.nleaf = nleaf;
+  g.nnode = nnode;
+  for (int l = 0; l < nleaf; l++) {
+    const pdlgb300_ndarray *x = leaves[l];
+    g.leaf[l] = opd[l].dev;
+    g.inc_n[l] = (n > 1 && x->ndims > 0 && x->dims[0] == n) ? x->incs[0] : 0;
+    g.lbad[l] = bad_bits(x);
+    g.lbad_isnan[l] = bad_isnan(x);
+    g.lflag[l] = lflag[l];
+  }
+  for (int k = 0; k < nnode; k++) g.nflag[k] = nflag[k];
+  g.tbad = bad_bits(&root);
+  g.tbad_isnan = bad_isnan(&root);
+  g.bad = rootflag;
+  g.out = opd[EXPR_MAXL].dev;
+  g.obad = bad_bits(out);
+  g.n = n;
+  g.rows = g.L.total;
+  g.f32_comp = (int)g_opt_comp;
+  g.nsplit = 1;
+  const int nsm = pgh::num_sms();
+  int grid = 0, block = 256;
+  if (n * (int64_t)TSIZES[T] <= 32768) {
+    g.group = 32;
+    grid = (int)std::min<int64_t>((g.rows + 7) / 8, (int64_t)1 << 30);
+  } else {
+    g.group = 256;
+    int64_t units = g.rows;
+    if (g.rows < 2 * (int64_t)nsm && n >= 65536) {
+      const int64_t want = std::max<int64_t>(1, (int64_t)nsm * 4 / g.rows);
+      g.nsplit = (int)std::max<int64_t>(1, std::min<int64_t>(want, n / 8192));
+      units = g.rows * g.nsplit;
+    }
+    grid = (int)std::min<int64_t>(units, (int64_t)1 << 30);
+  }
+  tl_info.rows = g.rows;
+  tl_info.n = n;
+  tl_info.datatype = T;
+  tl_info.bytes = (double)g.rows * n * TSIZES[T] * nleaf + (double)g.rows * TSIZES[out->datatype];
+  const bool minmax = redop == R_MIN || redop == R_MAX || redop == R_MIN_IND || redop == R_MAX_IND;
+  const bool need_flag = minmax && (rootflag || n == 0);
+  int *d_setbad = nullptr;
+  if (!e.error) e = setbad_word(&d_setbad);
+  g.setbad = d_setbad;
+  if (!e.error && need_flag) {
+    cudaError_t ce = cudaMemsetAsync(d_setbad, 0, sizeof(int), g_stream);
+    if (ce != cudaSuccess) e = err(PDLGB300_EFATAL, "clearing the bad flag: %s", cudaGetErrorString(ce));
+  }
+  void *scratch = nullptr;
+  RedArgs ra;
+  memset(&ra, 0, sizeof ra);
+  if (!e.error && g.nsplit > 1) {
+    const size_t accsz = expr_acc_size(redop, T, g.f32_comp);
+    const size_t npart = (size_t)g.rows * g.nsplit;
+    const size_t off = (npart * accsz + 15) & ~(size_t)15;
+    e = dalloc(off + npart * sizeof(int64_t) + 256, &scratch);
+    if (!e.error) {
+      g.partials = scratch;
+      g.pcounts = (int64_t *)((char *)scratch + off);
+      const int w2[2] = {0, EXPR_MAXL};
+      ra.L = collapse(b, 2, w2);
+      ra.b = g.out;
+      ra.rows = g.rows;
+      ra.n = n;
+      ra.inc_n = 1;
+      ra.nsplit = g.nsplit;
+      ra.partials = g.partials;
+      ra.pcounts = g.pcounts;
+      ra.bad = g.bad;
+      ra.bbad_bits = g.obad;
+      ra.setbad = d_setbad;
+    }
+  }
+  if (!e.error && g.rows > 0) {
+    Timer t;
+    t.start();
+    e = launch_expr_reduce(redop, T, g, ra, grid, block, g_stream);
+    tl_info.kernel_ms += t.stop();
+  }
+  if (scratch) cudaFreeAsync(scratch, g_stream);
+  int setbad = 0;
+  if (!e.error) {
+    if (need_flag) {
+      cudaError_t ce = cudaMemcpyAsync(&setbad, d_setbad, sizeof(int), cudaMemcpyDeviceToHost, g_stream);
+      if (ce == cudaSuccess) ce = cudaStreamSynchronize(g_stream);
+      if (ce != cudaSuccess) e = err(PDLGB300_EFATAL, "reading bad flags: %s", cudaGetErrorString(ce));
+    }
+    if (!e.error) e = unstage(opd[EXPR_MAXL]);
+  }
+  bool sync = false;
+  for (int i = 0; i <= EXPR_MAXL; i++) {
+    sync |= opd[i].to_host || opd[i].owned;
+    if (opd[i].owned) cudaFreeAsync(opd[i].owned, g_stream);
+  }
+  if (sync) {
+    cudaError_t ce = cudaStreamSynchronize(g_stream);
+    if (!e.error && ce != cudaSuccess) e = err(PDLGB300_EFATAL, "%s: %s", rvt->name, cudaGetErrorString(ce));
+  }
+  if (e.error) return e;
+  if (rootflag || setbad) out->state |= PDLGB300_BADVAL;
+  tl_last = tl_info;
+  return ok();
+}
+
 }  // namespace
 
 // ================================================================ C ABI
@@ -1481,6 +1743,16 @@ pdlgb300_error pdlgb300_run_minmaximum(pdlgb300_ndarray *a, pdlgb300_ndarray *cm
                                        pdlgb300_ndarray *cmax_ind) {
   pdlgb300_ndarray *p[5] = {a, cmin, cmax, cmin_ind, cmax_ind};
   return guard_run(O_MINMAXIMUM, p, nullptr);
+}
+
+pdlgb300_error pdlgb300_run_expr_reduce(const pdlgb300_vtable *reduction, int32_t nleaf,
+                                        pdlgb300_ndarray *const *leaves, int32_t nnode,
+                                        const pdlgb300_expr_node *nodes, pdlgb300_ndarray *out) {
+  try {
+    return run_expr_impl(reduction, nleaf, leaves, nnode, nodes, out);
+  } catch (...) {
+    return err(PDLGB300_EFATAL, "expression reduction: internal error");
+  }
 }
 
 pdlgb300_error pdlgb300_run_plus(pdlgb300_ndarray *a, pdlgb300_ndarray *b, pdlgb300_ndarray *c,

@@ -40,11 +40,43 @@ struct RedArgs {
                       // nullptr for a separate combine kernel
 };
 
+// A deferred expression reduced over dim 0 (expr.cu).  Operand indices:
+// 0..EXPR_MAXL-1 the leaves, EXPR_MAXL + k node k; node nnode-1 is the root.
+constexpr int EXPR_MAXL = 4, EXPR_MAXN = 8;
+struct ExprNode {
+  int op;    // BiopCode
+  int a, b;  // operands
+};
+struct ExprArgs {
+  Loop L;                          // pdls 0..EXPR_MAXL-1 leaves, EXPR_MAXL the output
+  const char *leaf[EXPR_MAXL];     // element (0) of each leaf
+  int64_t inc_n[EXPR_MAXL];        // each leaf's increment along dim 0 (0: broadcast)
+  uint64_t lbad[EXPR_MAXL];        // leaves' badvalues (raw bits)
+  int lbad_isnan[EXPR_MAXL], lflag[EXPR_MAXL];  // NaN badvalue; the leaf's bad flag
+  int nleaf, nnode;
+  ExprNode node[EXPR_MAXN];
+  int nflag[EXPR_MAXN];            // each node's bad flag (OR of its operands')
+  uint64_t tbad;                   // nodes' badvalue: the default of the type
+  int tbad_isnan;
+  int bad;                         // the reduction's bvalflag (the root's flag)
+  char *out;                       // element (0) of the output
+  uint64_t obad;
+  int64_t n, rows;
+  int group, nsplit, f32_comp;
+  void *partials;
+  int64_t *pcounts;
+  int *setbad;
+};
+bool expr_fusable(int redop, int dt);
+size_t expr_acc_size(int redop, int dt, int comp);
+
 struct RedLaunch {
   int kind;  // 0 rows, 1 thread
   int grid, block;
 };
 
+pdlgb300_error launch_expr_reduce(int redop, int dt, const ExprArgs &g, const RedArgs &ra,
+                                  int grid, int block, cudaStream_t s);
 pdlgb300_error launch_red_sum(int op, int in_dt, RedArgs args, const RedLaunch &lc,
                               cudaStream_t s);
 pdlgb300_error launch_red_prod(int op, int in_dt, RedArgs args, const RedLaunch &lc,

@@ -1,0 +1,272 @@
+// expr.cuh -- a deferred elementwise expression of PDL::Ops binary ops
+// (lib/PDL/Ops.pd:104-153, 288-307) over up to four broadcast leaves,
+// reduced over dim 0 by one of the PDL::Ufunc reductions
+// (lib/PDL/Ufunc.pd:94-187, 413-500) in one pass: the intermediates are
+// never written to memory.
+//
+// Every element of every intermediate is computed as the unfused ops
+// compute it: all leaves and intermediates have one type T (the host fuses
+// nothing else), each op rounds or wraps in T, and the bad-value rule of
+// each op is applied in turn -- an operand is bad when its ndarray has the
+// bad flag and its value equals its badvalue; a node's bad flag is the OR
+// of its operands' flags and its badvalue is T's default, exactly as a
+// materialised intermediate would have them.
+//
+// The program is uniform across the launch, so the per-node switches and
+// operand selections are uniform branches and selects on registers.  One
+// group of threads per output row (a warp for rows up to 32 KiB of T, a
+// block otherwise); few long rows split over several blocks whose partial
+// accumulators the row reduction's combine kernel merges.
+#pragma once
+#include "biop.cuh"
+#include "reduce.cuh"
+
+namespace pg {
+namespace {
+
+constexpr int NV = EXPR_MAXL + EXPR_MAXN;
+
+// v[i] for a runtime i below `lim` (a chain of selects on registers).
+template <class T, int LIM>
+__device__ __forceinline__ T pick(const T (&v)[NV], int i) {
+  T r = v[0];
+#pragma unroll
+  for (int c = 1; c < LIM; c++)
+    if (i == c) r = v[c];
+  return r;
+}
+template <int LIM>
+__device__ __forceinline__ bool pickb(const bool (&v)[NV], int i) {
+  bool r = v[0];
+#pragma unroll
+  for (int c = 1; c < LIM; c++)
+    if (i == c) r = v[c];
+  return r;
+}
+
+template <class T>
+__device__ __forceinline__ T apply_code(int op, T a, T b) {
+  switch (op) {
+    case B_PLUS: return biop_apply<T, B_PLUS>(a, b);
+    case B_MULT: return biop_apply<T, B_MULT>(a, b);
+    case B_MINUS: return biop_apply<T, B_MINUS>(a, b);
+    case B_DIVIDE: return biop_apply<T, B_DIVIDE>(a, b);
+    case B_GT: return biop_apply<T, B_GT>(a, b);
+    case B_LT: return biop_apply<T, B_LT>(a, b);
+    case B_LE: return biop_apply<T, B_LE>(a, b);
+    case B_GE: return biop_apply<T, B_GE>(a, b);
+    case B_EQ: return biop_apply<T, B_EQ>(a, b);
+    case B_NE: return biop_apply<T, B_NE>(a, b);
+    default: break;
+  }
+  if constexpr (std::is_integral_v<T>) {
+    switch (op) {
+      case B_SHL: return biop_apply<T, B_SHL>(a, b);
+      case B_SHR: return biop_apply<T, B_SHR>(a, b);
+      case B_OR2: return biop_apply<T, B_OR2>(a, b);
+      case B_AND2: return biop_apply<T, B_AND2>(a, b);
+      case B_XOR: return biop_apply<T, B_XOR>(a, b);
+      default: break;
+    }
+  }
+  return a;  // not reached: the host validates the program
+}
+
+// Node K and the nodes after it (K is a template argument so that the
+// operand selections stay on registers).
+template <class T, bool BAD, int K>
+__device__ __forceinline__ void node_step(const ExprArgs &g, T (&v)[NV], bool (&b)[NV],
+                                          const Bad<T> &tb) {
+  if constexpr (K < EXPR_MAXN) {
+    if (K >= g.nnode) return;
+    const ExprNode nd = g.node[K];
+    const T x = pick<T, EXPR_MAXL + K>(v, nd.a), y = pick<T, EXPR_MAXL + K>(v, nd.b);
+    T r;
+    if constexpr (BAD) {
+      const bool bx = pickb<EXPR_MAXL + K>(b, nd.a), by = pickb<EXPR_MAXL + K>(b, nd.b);
+      r = (bx || by) ? tb.val : apply_code<T>(nd.op, x, y);
+      b[EXPR_MAXL + K] = g.nflag[K] && tb.is(r);
+    } else {
+      r = apply_code<T>(nd.op, x, y);
+    }
+    v[EXPR_MAXL + K] = r;
+    node_step<T, BAD, K + 1>(g, v, b, tb);
+  }
+}
+
+// Element t of the expression; returns false when it is bad.
+template <class T, bool BAD>
+__device__ __forceinline__ bool expr_eval(const ExprArgs &g, const T (&leaf)[EXPR_MAXL],
+                                          const bool (&leafbad)[EXPR_MAXL], T &out) {
+  T v[NV];
+  bool b[NV];
+#pragma unroll
+  for (int l = 0; l < EXPR_MAXL; l++) {
+    v[l] = leaf[l];
+    b[l] = BAD && leafbad[l];
+  }
+#pragma unroll
+  for (int k = 0; k < EXPR_MAXN; k++) {
+    v[EXPR_MAXL + k] = (T)0;
+    b[EXPR_MAXL + k] = false;
+  }
+  const Bad<T> tb{from_bits<T>(g.tbad), (bool)g.tbad_isnan};
+  node_step<T, BAD, 0>(g, v, b, tb);
+  out = pick<T, NV>(v, EXPR_MAXL + g.nnode - 1);
+  return !(BAD && pickb<NV>(b, EXPR_MAXL + g.nnode - 1));
+}
+
+template <class T, bool BAD>
+__device__ __forceinline__ void load_leaves(const ExprArgs &g, const T *const (&p)[EXPR_MAXL],
+                                            int64_t t, T (&leaf)[EXPR_MAXL],
+                                            bool (&leafbad)[EXPR_MAXL]) {
+#pragma unroll
+  for (int l = 0; l < EXPR_MAXL; l++) {
+    leaf[l] = (T)0;
+    leafbad[l] = false;
+    if (l < g.nleaf) {
+      leaf[l] = p[l][t * g.inc_n[l]];
+      if constexpr (BAD)
+        leafbad[l] = g.lflag[l] && Bad<T>{from_bits<T>(g.lbad[l]), (bool)g.lbad_isnan[l]}.is(leaf[l]);
+    }
+  }
+}
+
+template <class Op, class T, class Out, bool BAD>
+__global__ void __launch_bounds__(256) k_expr_rows(const ExprArgs g) {
+  using Acc = typename Op::Acc;
+  using AC = AccCnt<Acc>;
+  const int G = g.group;
+  const int lane = G <= 32 ? (threadIdx.x & 31) : threadIdx.x;
+  const int gpb = G <= 32 ? (blockDim.x >> 5) : 1;
+  const int gid = G <= 32 ? (threadIdx.x >> 5) : 0;
+  const Out obad = from_bits<Out>(g.obad);
+  const int64_t nunits = g.rows * g.nsplit;
+  for (int64_t u = (int64_t)blockIdx.x * gpb + gid; u < nunits; u += (int64_t)gridDim.x * gpb) {
+    const int64_t row = u / g.nsplit;
+    const int split = (int)(u - row * g.nsplit);
+    int64_t offs[MAXP];
+    loop_offsets(g.L, row, offs);
+    const T *p[EXPR_MAXL];
+#pragma unroll
+    for (int l = 0; l < EXPR_MAXL; l++)
+      p[l] = reinterpret_cast<const T *>(g.leaf[l]) + (l < g.nleaf ? offs[l] : 0);
+    int64_t lo = 0, hi = g.n;
+    if (g.nsplit > 1) {
+      int64_t chunk = (g.n + g.nsplit - 1) / g.nsplit;
+      chunk = (chunk + 31) & ~(int64_t)31;
+      lo = split * chunk;
+      hi = lo + chunk < g.n ? lo + chunk : g.n;
+      if (lo > hi) lo = hi;
+    }
+    AC ac{Op::init(), 0};
+    // two elements per lane in flight: the leaves' loads first
+    constexpr int U = 2;
+    int64_t t = lo + lane;
+    for (; t + (U - 1) * (int64_t)G < hi; t += U * (int64_t)G) {
+      T leaf[U][EXPR_MAXL];
+      bool lb[U][EXPR_MAXL];
+#pragma unroll
+      for (int q = 0; q < U; q++) load_leaves<T, BAD>(g, p, t + q * (int64_t)G, leaf[q], lb[q]);
+#pragma unroll
+      for (int q = 0; q < U; q++) {
+        T v;
+        if (expr_eval<T, BAD>(g, leaf[q], lb[q], v)) {
+          Op::add(ac.acc, v, t + q * (int64_t)G);
+          ac.cnt++;
+        }
+      }
+    }
+    for (; t < hi; t += G) {
+      T leaf[EXPR_MAXL];
+      bool lb[EXPR_MAXL];
+      load_leaves<T, BAD>(g, p, t, leaf, lb);
+      T v;
+      if (expr_eval<T, BAD>(g, leaf, lb, v)) {
+        Op::add(ac.acc, v, t);
+        ac.cnt++;
+      }
+    }
+    ac = group_reduce<Op>(ac, G);
+    if (lane == 0) {
+      if (g.nsplit > 1) {
+        reinterpret_cast<Acc *>(g.partials)[u] = ac.acc;
+        g.pcounts[u] = ac.cnt;
+      } else {
+        Out r = Op::fin(ac.acc, ac.cnt, BAD, obad, g.setbad);
+        *(reinterpret_cast<Out *>(g.out) + offs[EXPR_MAXL]) = r;
+      }
+    }
+  }
+}
+
+template <class Op, class T, class Out>
+pdlgb300_error go(const ExprArgs &g, const RedArgs &ra, int grid, int block, cudaStream_t s) {
+  pdlgb300_error e = pgh::ok();
+  if (g.bad) k_expr_rows<Op, T, Out, true><<<grid, block, 0, s>>>(g);
+  else k_expr_rows<Op, T, Out, false><<<grid, block, 0, s>>>(g);
+  if (!pgh::cuda_check(cudaGetLastError(), &e, "k_expr_rows")) return e;
+  pgh::record_kernel("k_expr_rows", grid, block);
+  if (g.nsplit > 1) {
+    const int gc = (int)std::min<int64_t>((g.rows + 3) / 4, 65535);
+    if (g.bad) k_red_combine<Op, T, Out, true><<<gc, 128, 0, s>>>(ra);
+    else k_red_combine<Op, T, Out, false><<<gc, 128, 0, s>>>(ra);
+    if (!pgh::cuda_check(cudaGetLastError(), &e, "k_red_combine")) return e;
+    pgh::record_kernel("k_red_combine", gc, 128);
+  }
+  return e;
+}
+
+template <int DT>
+pdlgb300_error expr_family(int op, const ExprArgs &g, const RedArgs &ra, int grid, int block,
+                           cudaStream_t s) {
+  using T = typename TT<DT>::T;
+  using OutP = typename TT<intplus(DT)>::T;
+  constexpr bool F32 = std::is_same_v<OutP, float>;
+  constexpr bool INT = std::is_integral_v<T>;
+  switch (op) {
+    case R_SUM:
+      if constexpr (F32)
+        if (g.f32_comp) return go<OpSum<T, OutP, true>, T, OutP>(g, ra, grid, block, s);
+      return go<OpSum<T, OutP, false>, T, OutP>(g, ra, grid, block, s);
+    case R_DSUM: return go<OpSum<T, double, false>, T, double>(g, ra, grid, block, s);
+    case R_AVG:
+      if constexpr (F32)
+        if (g.f32_comp) return go<OpAvg<T, OutP, true>, T, OutP>(g, ra, grid, block, s);
+      return go<OpAvg<T, OutP, false>, T, OutP>(g, ra, grid, block, s);
+    case R_DAVG: return go<OpAvg<T, double, false>, T, double>(g, ra, grid, block, s);
+    case R_PROD:
+      if constexpr (INT) return go<OpProd<T, OutP>, T, OutP>(g, ra, grid, block, s);
+      break;
+    case R_MIN: return go<OpMM<T, false, false>, T, T>(g, ra, grid, block, s);
+    case R_MAX: return go<OpMM<T, true, false>, T, T>(g, ra, grid, block, s);
+    case R_MIN_IND: return go<OpMM<T, false, true>, T, int64_t>(g, ra, grid, block, s);
+    case R_MAX_IND: return go<OpMM<T, true, true>, T, int64_t>(g, ra, grid, block, s);
+    case R_AND: return go<OpLogic<T, 0>, T, T>(g, ra, grid, block, s);
+    case R_OR: return go<OpLogic<T, 1>, T, T>(g, ra, grid, block, s);
+    case R_XOR: return go<OpLogic<T, 2>, T, T>(g, ra, grid, block, s);
+    case R_ZC: return go<OpLogic<T, 3>, T, T>(g, ra, grid, block, s);
+    case R_BAND:
+      if constexpr (INT) return go<OpLogic<T, 4>, T, T>(g, ra, grid, block, s);
+      break;
+    case R_BOR:
+      if constexpr (INT) return go<OpLogic<T, 5>, T, T>(g, ra, grid, block, s);
+      break;
+    case R_BXOR:
+      if constexpr (INT) return go<OpLogic<T, 6>, T, T>(g, ra, grid, block, s);
+      break;
+    default: break;
+  }
+  return pgh::err(PDLGB300_EUSERERROR, "expression reduction %d: not fusable for type %d", op, DT);
+}
+
+}  // namespace
+
+// One instantiation per type, each in its own translation unit (expr_*.cu).
+template <int DT>
+pdlgb300_error launch_expr_typed(int op, const ExprArgs &g, const RedArgs &ra, int grid, int block,
+                                 cudaStream_t s) {
+  return expr_family<DT>(op, g, ra, grid, block, s);
+}
+
+}  // namespace pg

@@ -1,0 +1,7 @@
+// expr_d.cu -- the fused expression reductions for D leaves.
+#include "expr.cuh"
+
+namespace pg {
+template pdlgb300_error launch_expr_typed<PDLGB300_D>(int, const ExprArgs &, const RedArgs &, int, int,
+                                                 cudaStream_t);
+}  // namespace pg

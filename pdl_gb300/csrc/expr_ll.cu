@@ -1,0 +1,7 @@
+// expr_ll.cu -- the fused expression reductions for LL leaves.
+#include "expr.cuh"
+
+namespace pg {
+template pdlgb300_error launch_expr_typed<PDLGB300_LL>(int, const ExprArgs &, const RedArgs &, int, int,
+                                                 cudaStream_t);
+}  // namespace pg

@@ -1,0 +1,44 @@
+"""Deferred expressions without a GPU: each recorded op is shaped and typed
+by the library's redodims (the eager op's broadcasting, type selection and
+error text), and the fused program lists each distinct leaf once."""
+import numpy as np
+import pytest
+
+import pdl_gb300 as P
+
+
+def test_shapes_types_and_program():
+    a = P.pdl(np.arange(12.0).reshape(3, 4))     # dims (4, 3)
+    b = P.pdl(np.ones(4))                         # dims (4,)
+    e = P.lazy(a) * b + a
+    assert isinstance(e, P.Lazy) and e.dims == (4, 3) and e.type == "double"
+    leaves, nodes = e._program()
+    assert len(leaves) == 2 and leaves[0] is a and leaves[1] is b
+    assert nodes == [("mult", 0, 1), ("plus", 2, 0)]
+    # the reversed operators put the scalar first, as swap does
+    r = 1.0 - P.lazy(a)
+    assert r.op == "minus" and r.b is a and r.a.ndims == 0
+
+
+def test_bad_flag_and_int_scalars():
+    x = P.pdl(np.arange(6, dtype=np.int32))
+    x.badflag(1)
+    e = P.lazy(x) + 3
+    assert e.type == "long" and e.badflag()
+    assert e._program()[0][1].type == "long"     # the int scalar takes x's type
+
+
+def test_mismatch_is_the_eager_error():
+    a = P.pdl(np.zeros((3, 4)))
+    with pytest.raises(P.PDLError, match="Mismatched implicit broadcast dimension 0: size 4 vs. 5"):
+        P.lazy(a) + P.pdl(np.zeros(5))
+
+
+def test_not_fused_programs():
+    a = P.pdl(np.zeros(4, np.uint8))
+    assert (P.lazy(a) + a)._program() is None                 # byte: not a fused type
+    xs = [P.pdl(np.zeros(4)) for _ in range(5)]
+    e = P.lazy(xs[0]) + xs[1] + xs[2] + xs[3] + xs[4]
+    assert e._program() is None                               # five leaves
+    f = P.lazy(P.pdl(np.zeros(4, np.float32))) + P.pdl(np.zeros(4))
+    assert f.type == "double" and f._program() is None        # a float leaf converted
