@@ -531,6 +531,18 @@ def bench_c2(args, P, torch, stream):
         ms = time_op(torch, stream, lambda: P.sumover_mult_plus(x, y, x, c), args.mm_steps + 7)
         out[name] = {"ms": ms, "gops": nops / (ms * 1e-3) / 1e9,
                      "gbs": nbytes / (ms * 1e-3) / 1e9, "kernel": kern}
+        # the same expression through the generic deferred-expression kernel
+        # (one warp per output row, no tile reuse) and eagerly, op by op
+        from pdl_gb300.lazy import _run_fused
+        e = P.lazy(x) * y + x
+        leaves, nodes = e._program()
+        ce = _run_fused("sumover", leaves, nodes, None)
+        P.sync()
+        same = bool(np.array_equal(ce.numpy(), c.numpy())) if name == "int32" else None
+        ms_e = time_op(torch, stream, lambda: _run_fused("sumover", leaves, nodes, ce), args.mm_steps + 7)
+        ms_g = time_op(torch, stream, lambda: P.sumover(P.plus(P.mult(x, y), x)), 3)
+        out[name].update({"expr_generic_ms": ms_e, "eager_chain_ms": ms_g,
+                          "expr_generic_equals_tiled": same})
     out["config"] = ("sumover(a*b+a): a (256,1,8192), b (256,512,1) -> (512,8192); "
                      "int32 U{-1000..1000} seed 2; float32 N(0,1) seed 3 with 2% BAD")
     out["bound"] = "int32 / fp32 pipe (3 ops per element evaluation, ~120 ops per byte)"

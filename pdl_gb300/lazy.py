@@ -57,6 +57,7 @@ class Lazy:
     """One recorded binary op over ndarrays and other recorded ops."""
 
     __slots__ = ("op", "a", "b", "dims", "datatype", "_badflag")
+    _deferred = True
 
     def __init__(self, op: str, a, b):
         if op not in BIOPS:
@@ -162,12 +163,25 @@ class Lazy:
     def _reduce(self, name: str, out=None) -> N.ndarray:
         o = None if out is None or isinstance(out, N._Null) else out
         prog = self._program()
+        if prog is not None and name == "sumover" and _is_mult_plus(prog):
+            # sumover(a*b + d): the tiled kernel of sumover_mult_plus
+            leaves, nodes = prog
+            (_, i, j), (_, _, k) = nodes
+            return N.sumover_mult_plus(leaves[i], leaves[j], leaves[k], o)
         if prog is not None and name in FUSED_REDUCTIONS:
             leaves, nodes = prog
             r = _run_fused(name, leaves, nodes, o)
             if r is not None:
                 return r
         return getattr(N, name)(self.materialize(), o) if o is not None else getattr(N, name)(self.materialize())
+
+
+def _is_mult_plus(prog) -> bool:
+    """mult of two leaves, then plus of that and a leaf: sumover_mult_plus."""
+    leaves, nodes = prog
+    nl = len(leaves)
+    return (len(nodes) == 2 and nodes[0][0] == "mult" and nodes[0][1] < nl and nodes[0][2] < nl
+            and nodes[1][0] == "plus" and nodes[1][1] == nl and nodes[1][2] < nl)
 
 
 def _like(x):
@@ -274,6 +288,7 @@ class LazyLeaf:
     """An ndarray whose binary ops are recorded (lazy(a) * b -> Lazy)."""
 
     __slots__ = ("x",)
+    _deferred = True
 
     def __init__(self, x: N.ndarray):
         self.x = x

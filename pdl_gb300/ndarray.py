@@ -86,6 +86,11 @@ class Storage:
 
 # ------------------------------------------------------------------ ndarray
 
+def _deferred(o) -> bool:
+    """o is a recorded expression: let its reflected operator record the op."""
+    return getattr(o, "_deferred", False)
+
+
 class ndarray:
     def __init__(self, storage: Storage, datatype: int, dims: Sequence[int],
                  incs: Optional[Sequence[int]] = None, offs: int = 0,
@@ -311,33 +316,33 @@ class ndarray:
 
     # -- operators (overloads call the functions by name, as PP.pm:1450)
     def __add__(self, o):
-        return plus(self, o)
+        return NotImplemented if _deferred(o) else plus(self, o)
 
     def __radd__(self, o):
-        return plus(self, o, swap=1)
+        return NotImplemented if _deferred(o) else plus(self, o, swap=1)
 
     def __mul__(self, o):
-        return mult(self, o)
+        return NotImplemented if _deferred(o) else mult(self, o)
 
     def __rmul__(self, o):
-        return mult(self, o, swap=1)
+        return NotImplemented if _deferred(o) else mult(self, o, swap=1)
 
     def __matmul__(self, o):
         return matmult(self, o)
 
-    def __sub__(self, o): return minus(self, o)
-    def __rsub__(self, o): return minus(self, o, swap=1)
-    def __truediv__(self, o): return divide(self, o)
-    def __rtruediv__(self, o): return divide(self, o, swap=1)
-    def __gt__(self, o): return gt(self, o)
-    def __lt__(self, o): return lt(self, o)
-    def __ge__(self, o): return ge(self, o)
-    def __le__(self, o): return le(self, o)
-    def __lshift__(self, o): return shiftleft(self, o)
-    def __rshift__(self, o): return shiftright(self, o)
-    def __or__(self, o): return or2(self, o)
-    def __and__(self, o): return and2(self, o)
-    def __xor__(self, o): return xor(self, o)
+    def __sub__(self, o): return NotImplemented if _deferred(o) else minus(self, o)
+    def __rsub__(self, o): return NotImplemented if _deferred(o) else minus(self, o, swap=1)
+    def __truediv__(self, o): return NotImplemented if _deferred(o) else divide(self, o)
+    def __rtruediv__(self, o): return NotImplemented if _deferred(o) else divide(self, o, swap=1)
+    def __gt__(self, o): return NotImplemented if _deferred(o) else gt(self, o)
+    def __lt__(self, o): return NotImplemented if _deferred(o) else lt(self, o)
+    def __ge__(self, o): return NotImplemented if _deferred(o) else ge(self, o)
+    def __le__(self, o): return NotImplemented if _deferred(o) else le(self, o)
+    def __lshift__(self, o): return NotImplemented if _deferred(o) else shiftleft(self, o)
+    def __rshift__(self, o): return NotImplemented if _deferred(o) else shiftright(self, o)
+    def __or__(self, o): return NotImplemented if _deferred(o) else or2(self, o)
+    def __and__(self, o): return NotImplemented if _deferred(o) else and2(self, o)
+    def __xor__(self, o): return NotImplemented if _deferred(o) else xor(self, o)
 
     # -- methods
     def sumover(self, out=None): return sumover(self, out)

@@ -27,7 +27,8 @@ def _oracle(e):
 
 def _check(e, red, what):
     got = getattr(e, red)()
-    assert P.last_launch_info()["op"].endswith("(expr)"), what
+    op = P.last_launch_info()["op"]
+    assert op.endswith("(expr)") or op == "sumover_mult_plus", (what, op)
     ref_in = _oracle(e)
     exp = O.run(red, [ref_in])[0]
     if got.type in ("float", "double") and red in ("sumover", "average", "dsumover", "daverage"):
@@ -123,12 +124,19 @@ def test_not_fused_gives_the_eager_result(gpu):
     assert np.array_equal(got.numpy(), P.sumover(P.plus(P.mult(x, x), x)).numpy())
 
 
-def test_fused_matches_the_fused_smp_kernel(gpu):
-    # the same expression through the dedicated sumover_mult_plus kernel
+def test_generic_kernel_matches_the_tiled_kernel(gpu):
+    # sumover(a*b + a) goes to the tiled sumover_mult_plus kernel; the
+    # generic expression kernel gives the same integers
+    from pdl_gb300.lazy import _run_fused
     rng = seeded(("lazy-smp",))
     a = rng.integers(-100, 100, size=(256, 1, 64)).astype(np.int32)
     b = rng.integers(-100, 100, size=(1, 128, 64)).astype(np.int32)
     x, y = P.pdl(a).to_device(), P.pdl(b).to_device()
-    got = (P.lazy(x) * y + x).sumover().numpy()
-    want = P.sumover_mult_plus(x, y, x).numpy()
-    assert np.array_equal(got, want)
+    e = P.lazy(x) * y + x
+    got = e.sumover().numpy()
+    assert P.last_launch_info()["op"] == "sumover_mult_plus"
+    leaves, nodes = e._program()
+    generic = _run_fused("sumover", leaves, nodes, None).numpy()
+    assert P.last_launch_info()["op"] == "sumover(expr)"
+    assert np.array_equal(got, generic)
+    assert np.array_equal(got, P.sumover(P.plus(P.mult(x, y), x)).numpy())
