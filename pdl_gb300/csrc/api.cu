@@ -1532,6 +1532,20 @@ pdlgb300_error run_expr_impl(const pdlgb300_vtable *rvt, int nleaf,
   g.rows = g.L.total;
   g.f32_comp = (int)g_opt_comp;
   g.nsplit = 1;
+  // 16-byte loads: every leaf contiguous along dim 0 with each row start
+  // 16-byte aligned (its base and all its broadcast increments), or constant
+  // along dim 0
+  {
+    const int64_t vec = 16 / (int64_t)TSIZES[T];
+    bool ok = n >= 2 * vec;
+    for (int l = 0; l < nleaf && ok; l++) {
+      if (g.inc_n[l] == 0) continue;
+      if (g.inc_n[l] != 1 || ((uintptr_t)g.leaf[l] & 15)) ok = false;
+      for (int k = 0; k < g.L.nd && ok; k++)
+        if (g.L.size[k] > 1 && g.L.inc[l][k] % vec) ok = false;
+    }
+    g.vec = ok;
+  }
   const int nsm = pgh::num_sms();
   int grid = 0, block = 256;
   if (n * (int64_t)TSIZES[T] <= 32768) {

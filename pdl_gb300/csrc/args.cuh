@@ -63,6 +63,7 @@ struct ExprArgs {
   uint64_t obad;
   int64_t n, rows;
   int group, nsplit, f32_comp;
+  int vec;                         // leaves contiguous (16-byte aligned rows) or constant along dim 0
   void *partials;
   int64_t *pcounts;
   int *setbad;

@@ -4,7 +4,7 @@
 
 namespace pg {
 
-template <int DT>
+template <int DT, bool VL>
 pdlgb300_error launch_expr_typed(int op, const ExprArgs &g, const RedArgs &ra, int grid, int block,
                                  cudaStream_t s);
 
@@ -31,10 +31,18 @@ size_t expr_acc_size(int op, int dt, int comp) {
 pdlgb300_error launch_expr_reduce(int op, int dt, const ExprArgs &g, const RedArgs &ra, int grid,
                                   int block, cudaStream_t s) {
   switch (dt) {
-    case PDLGB300_L: return launch_expr_typed<PDLGB300_L>(op, g, ra, grid, block, s);
-    case PDLGB300_LL: return launch_expr_typed<PDLGB300_LL>(op, g, ra, grid, block, s);
-    case PDLGB300_F: return launch_expr_typed<PDLGB300_F>(op, g, ra, grid, block, s);
-    case PDLGB300_D: return launch_expr_typed<PDLGB300_D>(op, g, ra, grid, block, s);
+    case PDLGB300_L:
+      return g.vec ? launch_expr_typed<PDLGB300_L, true>(op, g, ra, grid, block, s)
+                   : launch_expr_typed<PDLGB300_L, false>(op, g, ra, grid, block, s);
+    case PDLGB300_LL:
+      return g.vec ? launch_expr_typed<PDLGB300_LL, true>(op, g, ra, grid, block, s)
+                   : launch_expr_typed<PDLGB300_LL, false>(op, g, ra, grid, block, s);
+    case PDLGB300_F:
+      return g.vec ? launch_expr_typed<PDLGB300_F, true>(op, g, ra, grid, block, s)
+                   : launch_expr_typed<PDLGB300_F, false>(op, g, ra, grid, block, s);
+    case PDLGB300_D:
+      return g.vec ? launch_expr_typed<PDLGB300_D, true>(op, g, ra, grid, block, s)
+                   : launch_expr_typed<PDLGB300_D, false>(op, g, ra, grid, block, s);
     default: break;
   }
   return pgh::err(PDLGB300_EUSERERROR, "expression reduction: type %d is not fusable", dt);

@@ -160,24 +160,7 @@ __global__ void __launch_bounds__(256) k_expr_rows(const ExprArgs g) {
       if (lo > hi) lo = hi;
     }
     AC ac{Op::init(), 0};
-    // two elements per lane in flight: the leaves' loads first
-    constexpr int U = 2;
-    int64_t t = lo + lane;
-    for (; t + (U - 1) * (int64_t)G < hi; t += U * (int64_t)G) {
-      T leaf[U][EXPR_MAXL];
-      bool lb[U][EXPR_MAXL];
-#pragma unroll
-      for (int q = 0; q < U; q++) load_leaves<T, BAD>(g, p, t + q * (int64_t)G, leaf[q], lb[q]);
-#pragma unroll
-      for (int q = 0; q < U; q++) {
-        T v;
-        if (expr_eval<T, BAD>(g, leaf[q], lb[q], v)) {
-          Op::add(ac.acc, v, t + q * (int64_t)G);
-          ac.cnt++;
-        }
-      }
-    }
-    for (; t < hi; t += G) {
+    for (int64_t t = lo + lane; t < hi; t += G) {
       T leaf[EXPR_MAXL];
       bool lb[EXPR_MAXL];
       load_leaves<T, BAD>(g, p, t, leaf, lb);
@@ -200,13 +183,138 @@ __global__ void __launch_bounds__(256) k_expr_rows(const ExprArgs g) {
   }
 }
 
-template <class Op, class T, class Out>
+// Rows whose leaves are each contiguous along dim 0 (16-byte aligned at
+// every row start) or constant along it: the contiguous leaves are read with
+// 16-byte streaming loads, two vectors per lane in flight, and the constant
+// ones once per row.
+template <class Op, class T, class Out, bool BAD>
+__global__ void __launch_bounds__(256) k_expr_rows_vec(const ExprArgs g) {
+  using Acc = typename Op::Acc;
+  using AC = AccCnt<Acc>;
+  constexpr int VEC = 16 / sizeof(T);
+  using V = VecT<T, VEC>;
+  const int G = g.group;
+  const int lane = G <= 32 ? (threadIdx.x & 31) : threadIdx.x;
+  const int gpb = G <= 32 ? (blockDim.x >> 5) : 1;
+  const int gid = G <= 32 ? (threadIdx.x >> 5) : 0;
+  const Out obad = from_bits<Out>(g.obad);
+  const int64_t nunits = g.rows * g.nsplit;
+  for (int64_t u = (int64_t)blockIdx.x * gpb + gid; u < nunits; u += (int64_t)gridDim.x * gpb) {
+    const int64_t row = u / g.nsplit;
+    const int split = (int)(u - row * g.nsplit);
+    int64_t offs[MAXP];
+    loop_offsets(g.L, row, offs);
+    const T *p[EXPR_MAXL];
+    T cst[EXPR_MAXL];
+    bool cbad[EXPR_MAXL];
+#pragma unroll
+    for (int l = 0; l < EXPR_MAXL; l++) {
+      p[l] = reinterpret_cast<const T *>(g.leaf[l]) + (l < g.nleaf ? offs[l] : 0);
+      cst[l] = (T)0;
+      cbad[l] = false;
+      if (l < g.nleaf && g.inc_n[l] == 0) {
+        cst[l] = p[l][0];
+        if constexpr (BAD)
+          cbad[l] = g.lflag[l] && Bad<T>{from_bits<T>(g.lbad[l]), (bool)g.lbad_isnan[l]}.is(cst[l]);
+      }
+    }
+    int64_t lo = 0, hi = g.n;
+    if (g.nsplit > 1) {
+      int64_t chunk = (g.n + g.nsplit - 1) / g.nsplit;
+      chunk = (chunk + 31) & ~(int64_t)31;
+      lo = split * chunk;
+      hi = lo + chunk < g.n ? lo + chunk : g.n;
+      if (lo > hi) lo = hi;
+    }
+    AC ac{Op::init(), 0};
+    auto one = [&](const T (&leaf)[EXPR_MAXL], int64_t t) {
+      bool lb[EXPR_MAXL];
+#pragma unroll
+      for (int l = 0; l < EXPR_MAXL; l++) {
+        lb[l] = false;
+        if constexpr (BAD) {
+          if (l < g.nleaf)
+            lb[l] = g.inc_n[l] == 0 ? cbad[l]
+                                    : g.lflag[l] && Bad<T>{from_bits<T>(g.lbad[l]),
+                                                           (bool)g.lbad_isnan[l]}.is(leaf[l]);
+        }
+      }
+      T v;
+      if (expr_eval<T, BAD>(g, leaf, lb, v)) {
+        Op::add(ac.acc, v, t);
+        ac.cnt++;
+      }
+    };
+    // lo is a multiple of 32 elements, so every vector below is aligned;
+    // four elements per lane per iteration (code size: every element
+    // evaluation is unrolled)
+    const int64_t nvec = (hi - lo) / VEC;
+    constexpr int U = VEC >= 4 ? 1 : 4 / VEC;
+    int64_t q = lane;
+    for (; q + (U - 1) * (int64_t)G < nvec; q += U * (int64_t)G) {
+      V w[U][EXPR_MAXL];
+#pragma unroll
+      for (int k = 0; k < U; k++)
+#pragma unroll
+        for (int l = 0; l < EXPR_MAXL; l++)
+          if (l < g.nleaf && g.inc_n[l] != 0)
+            w[k][l] = ldv(reinterpret_cast<const V *>(p[l] + lo) + q + k * (int64_t)G);
+#pragma unroll
+      for (int k = 0; k < U; k++) {
+#pragma unroll
+        for (int e = 0; e < VEC; e++) {
+          T leaf[EXPR_MAXL];
+#pragma unroll
+          for (int l = 0; l < EXPR_MAXL; l++) leaf[l] = g.inc_n[l] != 0 ? w[k][l].e[e] : cst[l];
+          one(leaf, lo + (q + k * (int64_t)G) * VEC + e);
+        }
+      }
+    }
+    for (; q < nvec; q += G) {
+      V w[EXPR_MAXL];
+#pragma unroll
+      for (int l = 0; l < EXPR_MAXL; l++)
+        if (l < g.nleaf && g.inc_n[l] != 0) w[l] = ldv(reinterpret_cast<const V *>(p[l] + lo) + q);
+#pragma unroll
+      for (int e = 0; e < VEC; e++) {
+        T leaf[EXPR_MAXL];
+#pragma unroll
+        for (int l = 0; l < EXPR_MAXL; l++) leaf[l] = g.inc_n[l] != 0 ? w[l].e[e] : cst[l];
+        one(leaf, lo + q * VEC + e);
+      }
+    }
+    for (int64_t t = lo + nvec * VEC + lane; t < hi; t += G) {
+      T leaf[EXPR_MAXL];
+#pragma unroll
+      for (int l = 0; l < EXPR_MAXL; l++) leaf[l] = g.inc_n[l] != 0 ? p[l][t] : cst[l];
+      one(leaf, t);
+    }
+    ac = group_reduce<Op>(ac, G);
+    if (lane == 0) {
+      if (g.nsplit > 1) {
+        reinterpret_cast<Acc *>(g.partials)[u] = ac.acc;
+        g.pcounts[u] = ac.cnt;
+      } else {
+        Out r = Op::fin(ac.acc, ac.cnt, BAD, obad, g.setbad);
+        *(reinterpret_cast<Out *>(g.out) + offs[EXPR_MAXL]) = r;
+      }
+    }
+  }
+}
+
+template <class Op, class T, class Out, bool VL>
 pdlgb300_error go(const ExprArgs &g, const RedArgs &ra, int grid, int block, cudaStream_t s) {
   pdlgb300_error e = pgh::ok();
-  if (g.bad) k_expr_rows<Op, T, Out, true><<<grid, block, 0, s>>>(g);
-  else k_expr_rows<Op, T, Out, false><<<grid, block, 0, s>>>(g);
-  if (!pgh::cuda_check(cudaGetLastError(), &e, "k_expr_rows")) return e;
-  pgh::record_kernel("k_expr_rows", grid, block);
+  const char *nm = VL ? "k_expr_rows_vec" : "k_expr_rows";
+  if constexpr (VL) {
+    if (g.bad) k_expr_rows_vec<Op, T, Out, true><<<grid, block, 0, s>>>(g);
+    else k_expr_rows_vec<Op, T, Out, false><<<grid, block, 0, s>>>(g);
+  } else {
+    if (g.bad) k_expr_rows<Op, T, Out, true><<<grid, block, 0, s>>>(g);
+    else k_expr_rows<Op, T, Out, false><<<grid, block, 0, s>>>(g);
+  }
+  if (!pgh::cuda_check(cudaGetLastError(), &e, nm)) return e;
+  pgh::record_kernel(nm, grid, block);
   if (g.nsplit > 1) {
     const int gc = (int)std::min<int64_t>((g.rows + 3) / 4, 65535);
     if (g.bad) k_red_combine<Op, T, Out, true><<<gc, 128, 0, s>>>(ra);
@@ -217,7 +325,7 @@ pdlgb300_error go(const ExprArgs &g, const RedArgs &ra, int grid, int block, cud
   return e;
 }
 
-template <int DT>
+template <int DT, bool VL>
 pdlgb300_error expr_family(int op, const ExprArgs &g, const RedArgs &ra, int grid, int block,
                            cudaStream_t s) {
   using T = typename TT<DT>::T;
@@ -227,33 +335,33 @@ pdlgb300_error expr_family(int op, const ExprArgs &g, const RedArgs &ra, int gri
   switch (op) {
     case R_SUM:
       if constexpr (F32)
-        if (g.f32_comp) return go<OpSum<T, OutP, true>, T, OutP>(g, ra, grid, block, s);
-      return go<OpSum<T, OutP, false>, T, OutP>(g, ra, grid, block, s);
-    case R_DSUM: return go<OpSum<T, double, false>, T, double>(g, ra, grid, block, s);
+        if (g.f32_comp) return go<OpSum<T, OutP, true>, T, OutP, VL>(g, ra, grid, block, s);
+      return go<OpSum<T, OutP, false>, T, OutP, VL>(g, ra, grid, block, s);
+    case R_DSUM: return go<OpSum<T, double, false>, T, double, VL>(g, ra, grid, block, s);
     case R_AVG:
       if constexpr (F32)
-        if (g.f32_comp) return go<OpAvg<T, OutP, true>, T, OutP>(g, ra, grid, block, s);
-      return go<OpAvg<T, OutP, false>, T, OutP>(g, ra, grid, block, s);
-    case R_DAVG: return go<OpAvg<T, double, false>, T, double>(g, ra, grid, block, s);
+        if (g.f32_comp) return go<OpAvg<T, OutP, true>, T, OutP, VL>(g, ra, grid, block, s);
+      return go<OpAvg<T, OutP, false>, T, OutP, VL>(g, ra, grid, block, s);
+    case R_DAVG: return go<OpAvg<T, double, false>, T, double, VL>(g, ra, grid, block, s);
     case R_PROD:
-      if constexpr (INT) return go<OpProd<T, OutP>, T, OutP>(g, ra, grid, block, s);
+      if constexpr (INT) return go<OpProd<T, OutP>, T, OutP, VL>(g, ra, grid, block, s);
       break;
-    case R_MIN: return go<OpMM<T, false, false>, T, T>(g, ra, grid, block, s);
-    case R_MAX: return go<OpMM<T, true, false>, T, T>(g, ra, grid, block, s);
-    case R_MIN_IND: return go<OpMM<T, false, true>, T, int64_t>(g, ra, grid, block, s);
-    case R_MAX_IND: return go<OpMM<T, true, true>, T, int64_t>(g, ra, grid, block, s);
-    case R_AND: return go<OpLogic<T, 0>, T, T>(g, ra, grid, block, s);
-    case R_OR: return go<OpLogic<T, 1>, T, T>(g, ra, grid, block, s);
-    case R_XOR: return go<OpLogic<T, 2>, T, T>(g, ra, grid, block, s);
-    case R_ZC: return go<OpLogic<T, 3>, T, T>(g, ra, grid, block, s);
+    case R_MIN: return go<OpMM<T, false, false>, T, T, VL>(g, ra, grid, block, s);
+    case R_MAX: return go<OpMM<T, true, false>, T, T, VL>(g, ra, grid, block, s);
+    case R_MIN_IND: return go<OpMM<T, false, true>, T, int64_t, VL>(g, ra, grid, block, s);
+    case R_MAX_IND: return go<OpMM<T, true, true>, T, int64_t, VL>(g, ra, grid, block, s);
+    case R_AND: return go<OpLogic<T, 0>, T, T, VL>(g, ra, grid, block, s);
+    case R_OR: return go<OpLogic<T, 1>, T, T, VL>(g, ra, grid, block, s);
+    case R_XOR: return go<OpLogic<T, 2>, T, T, VL>(g, ra, grid, block, s);
+    case R_ZC: return go<OpLogic<T, 3>, T, T, VL>(g, ra, grid, block, s);
     case R_BAND:
-      if constexpr (INT) return go<OpLogic<T, 4>, T, T>(g, ra, grid, block, s);
+      if constexpr (INT) return go<OpLogic<T, 4>, T, T, VL>(g, ra, grid, block, s);
       break;
     case R_BOR:
-      if constexpr (INT) return go<OpLogic<T, 5>, T, T>(g, ra, grid, block, s);
+      if constexpr (INT) return go<OpLogic<T, 5>, T, T, VL>(g, ra, grid, block, s);
       break;
     case R_BXOR:
-      if constexpr (INT) return go<OpLogic<T, 6>, T, T>(g, ra, grid, block, s);
+      if constexpr (INT) return go<OpLogic<T, 6>, T, T, VL>(g, ra, grid, block, s);
       break;
     default: break;
   }
@@ -262,11 +370,12 @@ pdlgb300_error expr_family(int op, const ExprArgs &g, const RedArgs &ra, int gri
 
 }  // namespace
 
-// One instantiation per type, each in its own translation unit (expr_*.cu).
-template <int DT>
+// One instantiation per type and kernel variant, each in its own
+// translation unit (expr_<type>[v].cu), so that they compile in parallel.
+template <int DT, bool VL>
 pdlgb300_error launch_expr_typed(int op, const ExprArgs &g, const RedArgs &ra, int grid, int block,
                                  cudaStream_t s) {
-  return expr_family<DT>(op, g, ra, grid, block, s);
+  return expr_family<DT, VL>(op, g, ra, grid, block, s);
 }
 
 }  // namespace pg

@@ -1,7 +1,8 @@
-// expr_d.cu -- the fused expression reductions for D leaves.
+// expr_d.cu -- the fused expression reductions for D leaves
+// (strided or broadcast rows).
 #include "expr.cuh"
 
 namespace pg {
-template pdlgb300_error launch_expr_typed<PDLGB300_D>(int, const ExprArgs &, const RedArgs &, int, int,
-                                                 cudaStream_t);
+template pdlgb300_error launch_expr_typed<PDLGB300_D, false>(int, const ExprArgs &, const RedArgs &, int,
+                                                       int, cudaStream_t);
 }  // namespace pg

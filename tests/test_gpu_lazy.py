@@ -63,12 +63,15 @@ def test_smp_shape_all_reductions(gpu, t):
             _check(e, red, f"{red} {t}")
 
 
+@pytest.mark.parametrize("n", [333, 336])
 @pytest.mark.parametrize("t", TYPES)
-def test_bad_values_through_the_chain(gpu, t):
-    rng = seeded(("lazy-bad", t))
-    a, _ = rand_array(rng, t, (40, 333), -9, 9, bad_frac=0.1)
-    b, _ = rand_array(rng, t, (40, 333), -9, 9)
-    c, _ = rand_array(rng, t, (1, 333), 1, 9, bad_frac=0.05)
+def test_bad_values_through_the_chain(gpu, t, n):
+    """n = 333: rows not 16-byte aligned (element loads); 336: aligned rows
+    (16-byte loads)."""
+    rng = seeded(("lazy-bad", t, n))
+    a, _ = rand_array(rng, t, (40, n), -9, 9, bad_frac=0.1)
+    b, _ = rand_array(rng, t, (40, n), -9, 9)
+    c, _ = rand_array(rng, t, (1, n), 1, 9, bad_frac=0.05)
     x, y, z = to_pdl(a, t, badflag=True), to_pdl(b, t), to_pdl(c, t, badflag=True)
     e = (P.lazy(x) - y) * z
     for red in ["sumover", "average", "minimum", "maximum_ind", "orover"]:
@@ -133,10 +136,11 @@ def test_generic_kernel_matches_the_tiled_kernel(gpu):
     b = rng.integers(-100, 100, size=(1, 128, 64)).astype(np.int32)
     x, y = P.pdl(a).to_device(), P.pdl(b).to_device()
     e = P.lazy(x) * y + x
-    got = e.sumover().numpy()
+    got = e.sumover()
     assert P.last_launch_info()["op"] == "sumover_mult_plus"
     leaves, nodes = e._program()
-    generic = _run_fused("sumover", leaves, nodes, None).numpy()
+    generic = _run_fused("sumover", leaves, nodes, None)
     assert P.last_launch_info()["op"] == "sumover(expr)"
+    got, generic = got.numpy(), generic.numpy()
     assert np.array_equal(got, generic)
     assert np.array_equal(got, P.sumover(P.plus(P.mult(x, y), x)).numpy())
