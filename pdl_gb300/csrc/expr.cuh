@@ -184,20 +184,41 @@ __global__ void __launch_bounds__(256) k_expr_rows(const ExprArgs g) {
 }
 
 // Rows whose leaves are each contiguous along dim 0 (16-byte aligned at
-// every row start) or constant along it: the contiguous leaves are read with
-// 16-byte streaming loads, two vectors per lane in flight, and the constant
-// ones once per row.
+// every row start) or constant along it.  Each thread streams its own
+// 16-byte vectors of the contiguous leaves through a private ring of
+// EXPR_STAGES slots in shared memory with cp.async (EXPR_STAGES-1 vectors
+// per leaf in flight per thread, no registers held for them); the constant
+// leaves are read once per row.  Only the thread that copied a slot reads
+// it, so the ring needs no barrier: cp.async.wait_group orders each
+// thread's own copies.
+constexpr int EXPR_STAGES = 4;
+
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void *src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N> __device__ __forceinline__ void cp_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
 template <class Op, class T, class Out, bool BAD>
 __global__ void __launch_bounds__(256) k_expr_rows_vec(const ExprArgs g) {
   using Acc = typename Op::Acc;
   using AC = AccCnt<Acc>;
   constexpr int VEC = 16 / sizeof(T);
+  constexpr int P = EXPR_STAGES;
   using V = VecT<T, VEC>;
+  extern __shared__ __align__(16) unsigned char xs_raw[];
   const int G = g.group;
   const int lane = G <= 32 ? (threadIdx.x & 31) : threadIdx.x;
   const int gpb = G <= 32 ? (blockDim.x >> 5) : 1;
   const int gid = G <= 32 ? (threadIdx.x >> 5) : 0;
   const Out obad = from_bits<Out>(g.obad);
+  const int nl = g.nleaf;
+  // slot (stage, leaf) of this thread: [stage][leaf][thread], 16 bytes each
+  const uint32_t ring = (uint32_t)__cvta_generic_to_shared(xs_raw) + threadIdx.x * 16u;
+  const uint32_t sstride = blockDim.x * 16u;
+  const V *ringp = reinterpret_cast<const V *>(xs_raw) + threadIdx.x;
   const int64_t nunits = g.rows * g.nsplit;
   for (int64_t u = (int64_t)blockIdx.x * gpb + gid; u < nunits; u += (int64_t)gridDim.x * gpb) {
     const int64_t row = u / g.nsplit;
@@ -209,10 +230,10 @@ __global__ void __launch_bounds__(256) k_expr_rows_vec(const ExprArgs g) {
     bool cbad[EXPR_MAXL];
 #pragma unroll
     for (int l = 0; l < EXPR_MAXL; l++) {
-      p[l] = reinterpret_cast<const T *>(g.leaf[l]) + (l < g.nleaf ? offs[l] : 0);
+      p[l] = reinterpret_cast<const T *>(g.leaf[l]) + (l < nl ? offs[l] : 0);
       cst[l] = (T)0;
       cbad[l] = false;
-      if (l < g.nleaf && g.inc_n[l] == 0) {
+      if (l < nl && g.inc_n[l] == 0) {
         cst[l] = p[l][0];
         if constexpr (BAD)
           cbad[l] = g.lflag[l] && Bad<T>{from_bits<T>(g.lbad[l]), (bool)g.lbad_isnan[l]}.is(cst[l]);
@@ -233,7 +254,7 @@ __global__ void __launch_bounds__(256) k_expr_rows_vec(const ExprArgs g) {
       for (int l = 0; l < EXPR_MAXL; l++) {
         lb[l] = false;
         if constexpr (BAD) {
-          if (l < g.nleaf)
+          if (l < nl)
             lb[l] = g.inc_n[l] == 0 ? cbad[l]
                                     : g.lflag[l] && Bad<T>{from_bits<T>(g.lbad[l]),
                                                            (bool)g.lbad_isnan[l]}.is(leaf[l]);
@@ -245,36 +266,28 @@ __global__ void __launch_bounds__(256) k_expr_rows_vec(const ExprArgs g) {
         ac.cnt++;
       }
     };
-    // lo is a multiple of 32 elements, so every vector below is aligned;
-    // four elements per lane per iteration (code size: every element
-    // evaluation is unrolled)
+    // lo is a multiple of 32 elements, so every vector below is aligned
     const int64_t nvec = (hi - lo) / VEC;
-    constexpr int U = VEC >= 4 ? 1 : 4 / VEC;
-    int64_t q = lane;
-    for (; q + (U - 1) * (int64_t)G < nvec; q += U * (int64_t)G) {
-      V w[U][EXPR_MAXL];
-#pragma unroll
-      for (int k = 0; k < U; k++)
+    auto issue = [&](int64_t q, int st) {
+      if (q < nvec) {
 #pragma unroll
         for (int l = 0; l < EXPR_MAXL; l++)
-          if (l < g.nleaf && g.inc_n[l] != 0)
-            w[k][l] = ldv(reinterpret_cast<const V *>(p[l] + lo) + q + k * (int64_t)G);
-#pragma unroll
-      for (int k = 0; k < U; k++) {
-#pragma unroll
-        for (int e = 0; e < VEC; e++) {
-          T leaf[EXPR_MAXL];
-#pragma unroll
-          for (int l = 0; l < EXPR_MAXL; l++) leaf[l] = g.inc_n[l] != 0 ? w[k][l].e[e] : cst[l];
-          one(leaf, lo + (q + k * (int64_t)G) * VEC + e);
-        }
+          if (l < nl && g.inc_n[l] != 0)
+            cp_async16(ring + (uint32_t)(st * nl + l) * sstride, p[l] + lo + q * VEC);
       }
-    }
-    for (; q < nvec; q += G) {
+      cp_commit();
+    };
+#pragma unroll
+    for (int s = 0; s < P - 1; s++) issue(lane + s * (int64_t)G, s);
+    int st = 0;
+    for (int64_t q = lane; q < nvec; q += G) {
+      cp_wait<P - 2>();  // this iteration's copies have landed
       V w[EXPR_MAXL];
 #pragma unroll
       for (int l = 0; l < EXPR_MAXL; l++)
-        if (l < g.nleaf && g.inc_n[l] != 0) w[l] = ldv(reinterpret_cast<const V *>(p[l] + lo) + q);
+        if (l < nl && g.inc_n[l] != 0) w[l] = ringp[(st * nl + l) * (int)blockDim.x];
+      // refill the slot read one iteration ago
+      issue(q + (P - 1) * (int64_t)G, st == 0 ? P - 1 : st - 1);
 #pragma unroll
       for (int e = 0; e < VEC; e++) {
         T leaf[EXPR_MAXL];
@@ -282,7 +295,9 @@ __global__ void __launch_bounds__(256) k_expr_rows_vec(const ExprArgs g) {
         for (int l = 0; l < EXPR_MAXL; l++) leaf[l] = g.inc_n[l] != 0 ? w[l].e[e] : cst[l];
         one(leaf, lo + q * VEC + e);
       }
+      st = st == P - 1 ? 0 : st + 1;
     }
+    cp_wait<0>();
     for (int64_t t = lo + nvec * VEC + lane; t < hi; t += G) {
       T leaf[EXPR_MAXL];
 #pragma unroll
@@ -307,8 +322,13 @@ pdlgb300_error go(const ExprArgs &g, const RedArgs &ra, int grid, int block, cud
   pdlgb300_error e = pgh::ok();
   const char *nm = VL ? "k_expr_rows_vec" : "k_expr_rows";
   if constexpr (VL) {
-    if (g.bad) k_expr_rows_vec<Op, T, Out, true><<<grid, block, 0, s>>>(g);
-    else k_expr_rows_vec<Op, T, Out, false><<<grid, block, 0, s>>>(g);
+    const int smem = EXPR_STAGES * g.nleaf * block * 16;
+    auto k = g.bad ? k_expr_rows_vec<Op, T, Out, true> : k_expr_rows_vec<Op, T, Out, false>;
+    if (smem > 48 * 1024 &&
+        !pgh::cuda_check(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem),
+                         &e, nm))
+      return e;
+    k<<<grid, block, smem, s>>>(g);
   } else {
     if (g.bad) k_expr_rows<Op, T, Out, true><<<grid, block, 0, s>>>(g);
     else k_expr_rows<Op, T, Out, false><<<grid, block, 0, s>>>(g);
