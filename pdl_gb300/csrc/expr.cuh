@@ -324,7 +324,8 @@ pdlgb300_error go(const ExprArgs &g, const RedArgs &ra, int grid, int block, cud
   if constexpr (VL) {
     const int smem = EXPR_STAGES * g.nleaf * block * 16;
     auto k = g.bad ? k_expr_rows_vec<Op, T, Out, true> : k_expr_rows_vec<Op, T, Out, false>;
-    if (smem > 48 * 1024 &&
+    // the default limit (48 KiB) includes the static shared memory
+    if (smem > 32 * 1024 &&
         !pgh::cuda_check(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem),
                          &e, nm))
       return e;
