@@ -76,7 +76,7 @@ __device__ __forceinline__ T apply_code(int op, T a, T b) {
 // operand selections stay on registers).
 template <class T, bool BAD, int K>
 __device__ __forceinline__ void node_step(const ExprArgs &g, T (&v)[NV], bool (&b)[NV],
-                                          const Bad<T> &tb) {
+                                          const Bad<T> &tb, T &last, bool &lastbad) {
   if constexpr (K < EXPR_MAXN) {
     if (K >= g.nnode) return;
     const ExprNode nd = g.node[K];
@@ -85,16 +85,18 @@ __device__ __forceinline__ void node_step(const ExprArgs &g, T (&v)[NV], bool (&
     if constexpr (BAD) {
       const bool bx = pickb<EXPR_MAXL + K>(b, nd.a), by = pickb<EXPR_MAXL + K>(b, nd.b);
       r = (bx || by) ? tb.val : apply_code<T>(nd.op, x, y);
-      b[EXPR_MAXL + K] = g.nflag[K] && tb.is(r);
+      lastbad = b[EXPR_MAXL + K] = g.nflag[K] && tb.is(r);
     } else {
       r = apply_code<T>(nd.op, x, y);
     }
-    v[EXPR_MAXL + K] = r;
-    node_step<T, BAD, K + 1>(g, v, b, tb);
+    last = v[EXPR_MAXL + K] = r;
+    node_step<T, BAD, K + 1>(g, v, b, tb, last, lastbad);
   }
 }
 
-// Element t of the expression; returns false when it is bad.
+// Element t of the expression; returns false when it is bad.  Node slots
+// are written before any later node can select them, so they need no
+// initial value; the last node evaluated is the result.
 template <class T, bool BAD>
 __device__ __forceinline__ bool expr_eval(const ExprArgs &g, const T (&leaf)[EXPR_MAXL],
                                           const bool (&leafbad)[EXPR_MAXL], T &out) {
@@ -105,15 +107,10 @@ __device__ __forceinline__ bool expr_eval(const ExprArgs &g, const T (&leaf)[EXP
     v[l] = leaf[l];
     b[l] = BAD && leafbad[l];
   }
-#pragma unroll
-  for (int k = 0; k < EXPR_MAXN; k++) {
-    v[EXPR_MAXL + k] = (T)0;
-    b[EXPR_MAXL + k] = false;
-  }
   const Bad<T> tb{from_bits<T>(g.tbad), (bool)g.tbad_isnan};
-  node_step<T, BAD, 0>(g, v, b, tb);
-  out = pick<T, NV>(v, EXPR_MAXL + g.nnode - 1);
-  return !(BAD && pickb<NV>(b, EXPR_MAXL + g.nnode - 1));
+  bool lastbad = false;
+  node_step<T, BAD, 0>(g, v, b, tb, out, lastbad);
+  return !(BAD && lastbad);
 }
 
 template <class T, bool BAD>

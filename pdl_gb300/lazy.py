@@ -126,13 +126,18 @@ class Lazy:
         leaves: List[N.ndarray] = []
         nodes = []
 
+        seen = {}
+
         def ref(x) -> Optional[int]:
             if isinstance(x, Lazy):
                 ia, ib = ref(x.a), ref(x.b)
                 if ia is None or ib is None:
                     return None
-                nodes.append((x.op, ia, ib))
-                return -len(nodes)  # node k is -(k+1) until the leaves are counted
+                key = (x.op, ia, ib)  # a repeated subexpression is computed once
+                if key not in seen:
+                    nodes.append(key)
+                    seen[key] = -len(nodes)  # node k is -(k+1) until the leaves are counted
+                return seen[key]
             for i, l in enumerate(leaves):
                 if l is x:
                     return i
