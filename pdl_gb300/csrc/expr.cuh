@@ -199,7 +199,7 @@ template <int N> __device__ __forceinline__ void cp_wait() {
 }
 
 template <class Op, class T, class Out, bool BAD>
-__global__ void __launch_bounds__(256) k_expr_rows_vec(const ExprArgs g) {
+__global__ void __launch_bounds__(256, 3) k_expr_rows_vec(const ExprArgs g) {
   using Acc = typename Op::Acc;
   using AC = AccCnt<Acc>;
   constexpr int VEC = 16 / sizeof(T);
@@ -244,8 +244,10 @@ __global__ void __launch_bounds__(256) k_expr_rows_vec(const ExprArgs g) {
       hi = lo + chunk < g.n ? lo + chunk : g.n;
       if (lo > hi) lo = hi;
     }
-    AC ac{Op::init(), 0};
-    auto one = [&](const T (&leaf)[EXPR_MAXL], int64_t t) {
+    // two accumulators (even and odd elements of a vector): two independent
+    // dependency chains per thread
+    AC ac{Op::init(), 0}, ac2{Op::init(), 0};
+    auto one = [&](const T (&leaf)[EXPR_MAXL], int64_t t, AC &a) {
       bool lb[EXPR_MAXL];
 #pragma unroll
       for (int l = 0; l < EXPR_MAXL; l++) {
@@ -259,8 +261,8 @@ __global__ void __launch_bounds__(256) k_expr_rows_vec(const ExprArgs g) {
       }
       T v;
       if (expr_eval<T, BAD>(g, leaf, lb, v)) {
-        Op::add(ac.acc, v, t);
-        ac.cnt++;
+        Op::add(a.acc, v, t);
+        a.cnt++;
       }
     };
     // lo is a multiple of 32 elements, so every vector below is aligned
@@ -290,7 +292,7 @@ __global__ void __launch_bounds__(256) k_expr_rows_vec(const ExprArgs g) {
         T leaf[EXPR_MAXL];
 #pragma unroll
         for (int l = 0; l < EXPR_MAXL; l++) leaf[l] = g.inc_n[l] != 0 ? w[l].e[e] : cst[l];
-        one(leaf, lo + q * VEC + e);
+        one(leaf, lo + q * VEC + e, (e & 1) ? ac2 : ac);
       }
       st = st == P - 1 ? 0 : st + 1;
     }
@@ -299,8 +301,9 @@ __global__ void __launch_bounds__(256) k_expr_rows_vec(const ExprArgs g) {
       T leaf[EXPR_MAXL];
 #pragma unroll
       for (int l = 0; l < EXPR_MAXL; l++) leaf[l] = g.inc_n[l] != 0 ? p[l][t] : cst[l];
-      one(leaf, t);
+      one(leaf, t, ac);
     }
+    merge_ac<Op>(ac, ac2);
     ac = group_reduce<Op>(ac, G);
     if (lane == 0) {
       if (g.nsplit > 1) {
