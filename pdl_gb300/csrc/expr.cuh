@@ -181,13 +181,16 @@ __global__ void __launch_bounds__(256) k_expr_rows(const ExprArgs g) {
 }
 
 // Rows whose leaves are each contiguous along dim 0 (16-byte aligned at
-// every row start) or constant along it.  Each thread streams its own
-// 16-byte vectors of the contiguous leaves through a private ring of
-// EXPR_STAGES slots in shared memory with cp.async (EXPR_STAGES-1 vectors
-// per leaf in flight per thread, no registers held for them); the constant
-// leaves are read once per row.  Only the thread that copied a slot reads
-// it, so the ring needs no barrier: cp.async.wait_group orders each
-// thread's own copies.
+// every row start) or constant along it: the program runs a 16-byte vector
+// at a time.  Each thread owns one column of shared memory slots (16 bytes
+// each): a ring of EXPR_STAGES slots per contiguous leaf that cp.async
+// fills ahead of use (EXPR_STAGES-1 vectors per leaf in flight), one slot
+// per constant leaf (its value broadcast, written once per row) and one per
+// node.  A node's operands are slot addresses (plain arithmetic on the
+// operand index) and its op is dispatched once per vector, so the per-
+// element work is the op itself.  In bad-value mode a 32-bit mask per slot
+// holds the elements' bad flags.  Only the thread that wrote a slot reads
+// it: no barriers; cp.async.wait_group orders each thread's own copies.
 constexpr int EXPR_STAGES = 4;
 
 __device__ __forceinline__ void cp_async16(uint32_t dst, const void *src) {
@@ -196,6 +199,47 @@ __device__ __forceinline__ void cp_async16(uint32_t dst, const void *src) {
 __device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 template <int N> __device__ __forceinline__ void cp_wait() {
   asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+template <class T, int VEC>
+__device__ __forceinline__ void apply_vec(int op, const VecT<T, VEC> &x, const VecT<T, VEC> &y,
+                                          VecT<T, VEC> &r) {
+#define PG_EXPR_CASE(C)                                             \
+  case C:                                                           \
+    _Pragma("unroll") for (int e = 0; e < VEC; e++)                 \
+        r.e[e] = biop_apply<T, C>(x.e[e], y.e[e]);                  \
+    return;
+  switch (op) {
+    PG_EXPR_CASE(B_PLUS)
+    PG_EXPR_CASE(B_MULT)
+    PG_EXPR_CASE(B_MINUS)
+    PG_EXPR_CASE(B_DIVIDE)
+    PG_EXPR_CASE(B_GT)
+    PG_EXPR_CASE(B_LT)
+    PG_EXPR_CASE(B_LE)
+    PG_EXPR_CASE(B_GE)
+    PG_EXPR_CASE(B_EQ)
+    PG_EXPR_CASE(B_NE)
+    default: break;
+  }
+  if constexpr (std::is_integral_v<T>) {
+    switch (op) {
+      PG_EXPR_CASE(B_SHL)
+      PG_EXPR_CASE(B_SHR)
+      PG_EXPR_CASE(B_OR2)
+      PG_EXPR_CASE(B_AND2)
+      PG_EXPR_CASE(B_XOR)
+      default: break;
+    }
+  }
+#undef PG_EXPR_CASE
+  r = x;  // not reached: the host validates the program
+}
+
+// Shared memory bytes of the vector kernel for a block of `block` threads.
+inline int expr_vec_smem(int nleaf, int nnode, int block, bool bad) {
+  const int slots = EXPR_STAGES * nleaf + nleaf + nnode;
+  return slots * block * 16 + (bad ? (nleaf + nnode) * block * 4 : 0);
 }
 
 template <class Op, class T, class Out, bool BAD>
@@ -211,11 +255,16 @@ __global__ void __launch_bounds__(256, 3) k_expr_rows_vec(const ExprArgs g) {
   const int gpb = G <= 32 ? (blockDim.x >> 5) : 1;
   const int gid = G <= 32 ? (threadIdx.x >> 5) : 0;
   const Out obad = from_bits<Out>(g.obad);
-  const int nl = g.nleaf;
-  // slot (stage, leaf) of this thread: [stage][leaf][thread], 16 bytes each
-  const uint32_t ring = (uint32_t)__cvta_generic_to_shared(xs_raw) + threadIdx.x * 16u;
-  const uint32_t sstride = blockDim.x * 16u;
-  const V *ringp = reinterpret_cast<const V *>(xs_raw) + threadIdx.x;
+  const int nl = g.nleaf, nn = g.nnode, bd = blockDim.x;
+  // this thread's column: slot i at col[i * bd]
+  V *const col = reinterpret_cast<V *>(xs_raw) + threadIdx.x;
+  V *const ring = col;                          // [stage][leaf]
+  V *const cslot = col + P * nl * bd;           // [leaf]
+  V *const nslot = cslot + nl * bd;             // [node]
+  uint32_t *const mcol = reinterpret_cast<uint32_t *>(
+      reinterpret_cast<V *>(xs_raw) + (P * nl + nl + nn) * bd) + threadIdx.x;  // [leaf], [node]
+  const uint32_t ring_sh = (uint32_t)__cvta_generic_to_shared(ring);
+  const Bad<T> tb{from_bits<T>(g.tbad), (bool)g.tbad_isnan};
   const int64_t nunits = g.rows * g.nsplit;
   for (int64_t u = (int64_t)blockIdx.x * gpb + gid; u < nunits; u += (int64_t)gridDim.x * gpb) {
     const int64_t row = u / g.nsplit;
@@ -223,17 +272,20 @@ __global__ void __launch_bounds__(256, 3) k_expr_rows_vec(const ExprArgs g) {
     int64_t offs[MAXP];
     loop_offsets(g.L, row, offs);
     const T *p[EXPR_MAXL];
-    T cst[EXPR_MAXL];
-    bool cbad[EXPR_MAXL];
 #pragma unroll
     for (int l = 0; l < EXPR_MAXL; l++) {
       p[l] = reinterpret_cast<const T *>(g.leaf[l]) + (l < nl ? offs[l] : 0);
-      cst[l] = (T)0;
-      cbad[l] = false;
       if (l < nl && g.inc_n[l] == 0) {
-        cst[l] = p[l][0];
-        if constexpr (BAD)
-          cbad[l] = g.lflag[l] && Bad<T>{from_bits<T>(g.lbad[l]), (bool)g.lbad_isnan[l]}.is(cst[l]);
+        const T c = p[l][0];
+        V cv;
+#pragma unroll
+        for (int e = 0; e < VEC; e++) cv.e[e] = c;
+        cslot[l * bd] = cv;
+        if constexpr (BAD) {
+          const bool cb =
+              g.lflag[l] && Bad<T>{from_bits<T>(g.lbad[l]), (bool)g.lbad_isnan[l]}.is(c);
+          mcol[l * bd] = cb ? (1u << VEC) - 1 : 0u;
+        }
       }
     }
     int64_t lo = 0, hi = g.n;
@@ -244,27 +296,7 @@ __global__ void __launch_bounds__(256, 3) k_expr_rows_vec(const ExprArgs g) {
       hi = lo + chunk < g.n ? lo + chunk : g.n;
       if (lo > hi) lo = hi;
     }
-    // two accumulators (even and odd elements of a vector): two independent
-    // dependency chains per thread
     AC ac{Op::init(), 0}, ac2{Op::init(), 0};
-    auto one = [&](const T (&leaf)[EXPR_MAXL], int64_t t, AC &a) {
-      bool lb[EXPR_MAXL];
-#pragma unroll
-      for (int l = 0; l < EXPR_MAXL; l++) {
-        lb[l] = false;
-        if constexpr (BAD) {
-          if (l < nl)
-            lb[l] = g.inc_n[l] == 0 ? cbad[l]
-                                    : g.lflag[l] && Bad<T>{from_bits<T>(g.lbad[l]),
-                                                           (bool)g.lbad_isnan[l]}.is(leaf[l]);
-        }
-      }
-      T v;
-      if (expr_eval<T, BAD>(g, leaf, lb, v)) {
-        Op::add(a.acc, v, t);
-        a.cnt++;
-      }
-    };
     // lo is a multiple of 32 elements, so every vector below is aligned
     const int64_t nvec = (hi - lo) / VEC;
     auto issue = [&](int64_t q, int st) {
@@ -272,7 +304,7 @@ __global__ void __launch_bounds__(256, 3) k_expr_rows_vec(const ExprArgs g) {
 #pragma unroll
         for (int l = 0; l < EXPR_MAXL; l++)
           if (l < nl && g.inc_n[l] != 0)
-            cp_async16(ring + (uint32_t)(st * nl + l) * sstride, p[l] + lo + q * VEC);
+            cp_async16(ring_sh + (uint32_t)((st * nl + l) * bd) * 16u, p[l] + lo + q * VEC);
       }
       cp_commit();
     };
@@ -281,27 +313,80 @@ __global__ void __launch_bounds__(256, 3) k_expr_rows_vec(const ExprArgs g) {
     int st = 0;
     for (int64_t q = lane; q < nvec; q += G) {
       cp_wait<P - 2>();  // this iteration's copies have landed
-      V w[EXPR_MAXL];
+      V *const stage = ring + st * nl * bd;
+      if constexpr (BAD) {
+        for (int l = 0; l < nl; l++) {
+          if (g.inc_n[l] == 0) continue;
+          const V w = stage[l * bd];
+          const Bad<T> lb{from_bits<T>(g.lbad[l]), (bool)g.lbad_isnan[l]};
+          uint32_t m = 0;
 #pragma unroll
-      for (int l = 0; l < EXPR_MAXL; l++)
-        if (l < nl && g.inc_n[l] != 0) w[l] = ringp[(st * nl + l) * (int)blockDim.x];
+          for (int e = 0; e < VEC; e++) m |= (g.lflag[l] && lb.is(w.e[e])) ? 1u << e : 0u;
+          mcol[l * bd] = m;
+        }
+      }
+      V last;
+      uint32_t lastm = 0;
+      for (int k = 0; k < nn; k++) {
+        const ExprNode nd = g.node[k];
+        // operand i: leaf i (ring slot of this stage, or its constant
+        // slot) or node i - EXPR_MAXL
+        auto at = [&](int i) -> const V & {
+          return i < EXPR_MAXL ? (g.inc_n[i] != 0 ? stage[i * bd] : cslot[i * bd])
+                               : nslot[(i - EXPR_MAXL) * bd];
+        };
+        const V x = at(nd.a), y = at(nd.b);
+        V r;
+        apply_vec<T, VEC>(nd.op, x, y, r);
+        if constexpr (BAD) {
+          auto mk = [&](int i) -> uint32_t {
+            return i < EXPR_MAXL ? mcol[i * bd] : mcol[(nl + i - EXPR_MAXL) * bd];
+          };
+          const uint32_t mb = mk(nd.a) | mk(nd.b);
+          uint32_t mr = 0;
+#pragma unroll
+          for (int e = 0; e < VEC; e++) {
+            if (mb >> e & 1u) r.e[e] = tb.val;
+            mr |= (g.nflag[k] && tb.is(r.e[e])) ? 1u << e : 0u;
+          }
+          mcol[(nl + k) * bd] = mr;
+          lastm = mr;
+        }
+        nslot[k * bd] = r;
+        last = r;
+      }
       // refill the slot read one iteration ago
       issue(q + (P - 1) * (int64_t)G, st == 0 ? P - 1 : st - 1);
+      const int64_t t0 = lo + q * VEC;
 #pragma unroll
       for (int e = 0; e < VEC; e++) {
-        T leaf[EXPR_MAXL];
-#pragma unroll
-        for (int l = 0; l < EXPR_MAXL; l++) leaf[l] = g.inc_n[l] != 0 ? w[l].e[e] : cst[l];
-        one(leaf, lo + q * VEC + e, (e & 1) ? ac2 : ac);
+        if (BAD && (lastm >> e & 1u)) continue;
+        AC &a = (e & 1) ? ac2 : ac;
+        Op::add(a.acc, last.e[e], t0 + e);
+        a.cnt++;
       }
       st = st == P - 1 ? 0 : st + 1;
     }
     cp_wait<0>();
+    // the ragged end: element by element through the register evaluator
     for (int64_t t = lo + nvec * VEC + lane; t < hi; t += G) {
       T leaf[EXPR_MAXL];
+      bool lb[EXPR_MAXL];
 #pragma unroll
-      for (int l = 0; l < EXPR_MAXL; l++) leaf[l] = g.inc_n[l] != 0 ? p[l][t] : cst[l];
-      one(leaf, t, ac);
+      for (int l = 0; l < EXPR_MAXL; l++) {
+        leaf[l] = (T)0;
+        lb[l] = false;
+        if (l < nl) {
+          leaf[l] = g.inc_n[l] != 0 ? p[l][t] : p[l][0];
+          if constexpr (BAD)
+            lb[l] = g.lflag[l] && Bad<T>{from_bits<T>(g.lbad[l]), (bool)g.lbad_isnan[l]}.is(leaf[l]);
+        }
+      }
+      T v;
+      if (expr_eval<T, BAD>(g, leaf, lb, v)) {
+        Op::add(ac.acc, v, t);
+        ac.cnt++;
+      }
     }
     merge_ac<Op>(ac, ac2);
     ac = group_reduce<Op>(ac, G);
@@ -322,7 +407,7 @@ pdlgb300_error go(const ExprArgs &g, const RedArgs &ra, int grid, int block, cud
   pdlgb300_error e = pgh::ok();
   const char *nm = VL ? "k_expr_rows_vec" : "k_expr_rows";
   if constexpr (VL) {
-    const int smem = EXPR_STAGES * g.nleaf * block * 16;
+    const int smem = expr_vec_smem(g.nleaf, g.nnode, block, g.bad);
     auto k = g.bad ? k_expr_rows_vec<Op, T, Out, true> : k_expr_rows_vec<Op, T, Out, false>;
     // the default limit (48 KiB) includes the static shared memory
     if (smem > 32 * 1024 &&
