@@ -573,9 +573,10 @@ def bench_expr(args, P, torch, stream, hbm):
     """A deferred expression reduced in one pass, HBM-bound: sumover((a-b)*(a-b))
     over float32 a, b dims (65536, 4096) N(0,1) (seed 8), against the same
     ops run eagerly (two materialised intermediates)."""
+    rows = args.expr_rows
     rng = np.random.default_rng(8)
-    a = rng.standard_normal((4096, 65536), dtype=np.float32)
-    b = rng.standard_normal((4096, 65536), dtype=np.float32)
+    a = rng.standard_normal((rows, 65536), dtype=np.float32)
+    b = rng.standard_normal((rows, 65536), dtype=np.float32)
     x, y = P.pdl(a).to_device(), P.pdl(b).to_device()
     del a, b
     d = P.lazy(x) - y
@@ -589,9 +590,9 @@ def bench_expr(args, P, torch, stream, hbm):
         t = P.minus(x, y)
         return P.sumover(P.mult(t, t))
     ms_eager = time_op(torch, stream, eager, 3)
-    nbytes = 2 * 4096 * 65536 * 4 + 4096 * 4
+    nbytes = 2 * rows * 65536 * 4 + rows * 4
     gbs = nbytes / (ms * 1e-3) / 1e9
-    return {"config": "sumover((a-b)*(a-b)), float32 a,b dims (65536,4096) N(0,1) seed 8 -> 4096",
+    return {"config": f"sumover((a-b)*(a-b)), float32 a,b dims (65536,{rows}) N(0,1) seed 8 -> {rows}",
             "ms": ms, "gbs": gbs, "frac_of_hbm": gbs / hbm, "op": op,
             "eager_ms": ms_eager, "speedup_vs_eager": ms_eager / ms}
 
@@ -672,6 +673,10 @@ def main():
                     help="skip the fused sumover(a*b+a) and float64 inner timings")
     ap.add_argument("--inner-cols", type=int, default=65536,
                     help="broadcast length of the float64 inner (smaller for profiling)")
+    ap.add_argument("--expr-rows", type=int, default=4096,
+                    help="rows of the deferred-expression workload (smaller for profiling)")
+    ap.add_argument("--expr-only", action="store_true",
+                    help="time only the deferred-expression workload and print its object")
     args = ap.parse_args()
     UFUNC_OPS = [o for o in args.ops.split(",") if o]
     rank = int(os.environ.get("RANK", 0))
@@ -680,6 +685,13 @@ def main():
         if rank != 0:
             return 0
         print(json.dumps(run_reference(args, rank, world)))
+        return 0
+    if args.expr_only:
+        import torch
+        import pdl_gb300 as P
+        stream = torch.cuda.current_stream()
+        P.set_stream(stream.cuda_stream)
+        print(json.dumps(bench_expr(args, P, torch, stream, peaks()[0])))
         return 0
     if world > 1:
         import torch
