@@ -182,6 +182,24 @@ pdlgb300_error pdlgb300_run_dcumuprodover(pdlgb300_ndarray *a, pdlgb300_ndarray 
 pdlgb300_error pdlgb300_run_minmaximum(pdlgb300_ndarray *a, pdlgb300_ndarray *cmin,
                                        pdlgb300_ndarray *cmax, pdlgb300_ndarray *cmin_ind,
                                        pdlgb300_ndarray *cmax_ind);
+/* lib/PDL/Ufunc.pd:744-1112, the sort-based functions, each with the
+ * reference's quicksort (lib/PDL/Core/pdl.h.PL:618-640) so that equal keys,
+ * NaN and signed zeros land where the reference puts them:
+ *   qsort a(n); [o]b(n)           -- bad values moved to the end (:1040-1077)
+ *   qsorti a(n); indx [o]indx(n)  -- bad indices from the end backwards (:1079-1112)
+ *   medover / oddmedover a(n); [o]b()  (:878-903)
+ *   pctover / oddpctover a(n); p(); [o]b()  (:975-1007)
+ *   modeover data(n); [o]out(), integer types (:905-939)
+ * medover .. oddpctover fail on an empty ndarray as the reference does.   */
+pdlgb300_error pdlgb300_run_qsort(pdlgb300_ndarray *a, pdlgb300_ndarray *b);
+pdlgb300_error pdlgb300_run_qsorti(pdlgb300_ndarray *a, pdlgb300_ndarray *indx);
+pdlgb300_error pdlgb300_run_medover(pdlgb300_ndarray *a, pdlgb300_ndarray *b);
+pdlgb300_error pdlgb300_run_oddmedover(pdlgb300_ndarray *a, pdlgb300_ndarray *b);
+pdlgb300_error pdlgb300_run_pctover(pdlgb300_ndarray *a, pdlgb300_ndarray *p,
+                                    pdlgb300_ndarray *b);
+pdlgb300_error pdlgb300_run_oddpctover(pdlgb300_ndarray *a, pdlgb300_ndarray *p,
+                                       pdlgb300_ndarray *b);
+pdlgb300_error pdlgb300_run_modeover(pdlgb300_ndarray *data, pdlgb300_ndarray *out);
 /* A deferred expression of PDL::Ops binary ops (lib/PDL/Ops.pd:104-153,
  * 288-307) reduced over dim 0 by a PDL::Ufunc reduction in one pass, with
  * the result the ops and the reduction give one after the other

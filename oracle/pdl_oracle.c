@@ -115,7 +115,8 @@ enum {
   OP_SHIFTRIGHT, OP_OR2, OP_AND2, OP_XOR,
   OP_ANDOVER, OP_OROVER, OP_XOROVER, OP_ZCOVER, OP_BANDOVER, OP_BOROVER,
   OP_BXOROVER, OP_FIRSTNONZEROOVER, OP_CUMUPRODOVER, OP_DCUMUPRODOVER,
-  OP_MINMAXIMUM,
+  OP_MINMAXIMUM, OP_QSORT, OP_QSORTI, OP_MEDOVER, OP_ODDMEDOVER, OP_PCTOVER,
+  OP_ODDPCTOVER, OP_MODEOVER,
   OP_N
 };
 #define IS_BIOP(op) ((op) == OP_PLUS || (op) == OP_MULT || ((op) >= OP_MINUS && (op) <= OP_XOR))
@@ -182,6 +183,14 @@ static const opdef OPS[OP_N] = {
   /* lib/PDL/Ufunc.pd:563-613 */
   {"minmaximum", 5, 1, {"a", "cmin", "cmax", "cmin_ind", "cmax_ind"}, {1, 0, 0, 0, 0},
    {{0}, {0}, {0}, {0}, {0}}, {"n"}, 0, -1, 0, 3},
+  /* lib/PDL/Ufunc.pd:878-1115: the sort-based functions */
+  {"qsort", 2, 1, {"a", "b"}, {1, 1}, {{0}, {0}}, {"n"}, 0, -1},
+  {"qsorti", 2, 1, {"a", "indx"}, {1, 1}, {{0}, {0}}, {"n"}, TYPED, PDLGB300_IND},
+  {"medover", 2, 1, {"a", "b"}, {1, 0}, {{0}, {0}}, {"n"}, 0, -1},
+  {"oddmedover", 2, 1, {"a", "b"}, {1, 0}, {{0}, {0}}, {"n"}, 0, -1},
+  {"pctover", 3, 2, {"a", "p", "b"}, {1, 0, 0}, {{0}, {0}, {0}}, {"n"}, 0, -1},
+  {"oddpctover", 3, 2, {"a", "p", "b"}, {1, 0, 0}, {{0}, {0}, {0}}, {"n"}, 0, -1},
+  {"modeover", 2, 1, {"data", "out"}, {1, 0}, {{0}, {0}}, {"n"}, 0, -1, 1},
 };
 
 static int find_op(const char *name) {
@@ -899,6 +908,208 @@ O_REAL_TYPES(DEF_INNERS)
 #define DEF_MATMULTS(E, CT, SYM, IP, ISF, UNS) DEF_MATMULT(matmult_##SYM, CT, SYM, ISF)
 O_REAL_TYPES(DEF_MATMULTS)
 
+/* ------------------------------------------------ sort-based (Ufunc.pd:744-1115)
+ * The sort is the quicksort of lib/PDL/Core/pdl.h.PL:618-640 (middle
+ * element as pivot, the two scans, swap, recurse on [a,j] then [i,b]); the
+ * two sub-ranges are disjoint, so recursing on the smaller one first and
+ * looping on the larger gives the same array with a bounded stack. */
+#define DEF_QSORT(T, SYM)                                                            \
+  static void oq_##SYM(T *xx, int64_t a, int64_t b) {                               \
+    while (a < b) {                                                                  \
+      int64_t i = a, j = b;                                                          \
+      T median = xx[(i + j) / 2];                                                    \
+      do {                                                                           \
+        while (xx[i] < median) i++;                                                  \
+        while (median < xx[j]) j--;                                                  \
+        if (i <= j) {                                                                \
+          T t = xx[i]; xx[i] = xx[j]; xx[j] = t;                                     \
+          i++; j--;                                                                  \
+        }                                                                            \
+      } while (i <= j);                                                              \
+      if (j - a < b - i) {                                                           \
+        if (a < j) oq_##SYM(xx, a, j);                                               \
+        a = i;                                                                       \
+      } else {                                                                       \
+        if (i < b) oq_##SYM(xx, i, b);                                               \
+        b = j;                                                                       \
+      }                                                                              \
+    }                                                                                \
+  }                                                                                  \
+  /* Ufunc.pd:745-767: the same on an index vector */                             \
+  static void oqi_##SYM(const T *xx, int64_t *ix, int64_t a, int64_t b) {           \
+    while (a < b) {                                                                  \
+      int64_t i = a, j = b;                                                          \
+      T median = xx[ix[(i + j) / 2]];                                                \
+      do {                                                                           \
+        while (xx[ix[i]] < median) i++;                                              \
+        while (median < xx[ix[j]]) j--;                                              \
+        if (i <= j) {                                                                \
+          int64_t t = ix[i]; ix[i] = ix[j]; ix[j] = t;                               \
+          i++; j--;                                                                  \
+        }                                                                            \
+      } while (i <= j);                                                              \
+      if (j - a < b - i) {                                                           \
+        if (a < j) oqi_##SYM(xx, ix, a, j);                                          \
+        a = i;                                                                       \
+      } else {                                                                       \
+        if (i < b) oqi_##SYM(xx, ix, i, b);                                          \
+        b = j;                                                                       \
+      }                                                                              \
+    }                                                                                \
+  }
+#define DEF_QSORTS(E, CT, SYM, IP, ISF, UNS) DEF_QSORT(CT, SYM)
+O_REAL_TYPES(DEF_QSORTS)
+
+/* the good elements of a row into tmp (all of them without bad values);
+ * returns their count (Ufunc.pd:857-867, $copy_to_temp) */
+#define DEF_SORTRED(T, SYM, ISF, UNS)                                                \
+  static int64_t sr_copy_##SYM(octx *c, const T *a, int64_t N, int64_t ia, T *tmp) { \
+    T abad = c->bad[0].SYM;                                                          \
+    int64_t nn = 0;                                                                  \
+    for (int64_t n = 0; n < N; n++) {                                                \
+      T v = a[n * ia];                                                               \
+      if (c->bvalflag && ISBADV(v, abad, ISF)) continue;                             \
+      tmp[nn++] = v;                                                                 \
+    }                                                                                \
+    return nn;                                                                       \
+  }                                                                                  \
+  static void qsort_##SYM(octx *c, const int64_t *offs, int64_t n0, const int64_t *inc0) { \
+    int64_t N = c->ind_sizes[0], ia = c->inc_sizes[0][0], ib = c->inc_sizes[1][0];   \
+    T *tmp = (T *)malloc(sizeof(T) * (N ? N : 1));                                   \
+    for (int64_t i0 = 0; i0 < n0; i0++) {                                            \
+      const T *a = (const T *)c->base[0] + offs[0] + i0 * inc0[0];                   \
+      T *b = (T *)c->base[1] + offs[1] + i0 * inc0[1];                               \
+      int64_t nn = sr_copy_##SYM(c, a, N, ia, tmp);                                  \
+      if (nn > 0) oq_##SYM(tmp, 0, nn - 1);                                          \
+      for (int64_t n = 0; n < N; n++) b[n * ib] = n < nn ? tmp[n] : c->bad[1].SYM;   \
+    }                                                                                \
+    free(tmp);                                                                       \
+  }                                                                                  \
+  /* Ufunc.pd:1079-1112: good indices in order, bad ones from the end */          \
+  static void qsorti_##SYM(octx *c, const int64_t *offs, int64_t n0, const int64_t *inc0) { \
+    int64_t N = c->ind_sizes[0], ia = c->inc_sizes[0][0], ib = c->inc_sizes[1][0];   \
+    T abad = c->bad[0].SYM;                                                          \
+    T *row = (T *)malloc(sizeof(T) * (N ? N : 1));                                   \
+    int64_t *ix = (int64_t *)malloc(sizeof(int64_t) * (N ? N : 1));                 \
+    for (int64_t i0 = 0; i0 < n0; i0++) {                                            \
+      const T *a = (const T *)c->base[0] + offs[0] + i0 * inc0[0];                   \
+      int64_t *b = (int64_t *)c->base[1] + offs[1] + i0 * inc0[1];                   \
+      int64_t nn = 0, nb = N - 1;                                                    \
+      for (int64_t n = 0; n < N; n++) {                                              \
+        row[n] = a[n * ia];                                                          \
+        if (c->bvalflag && ISBADV(row[n], abad, ISF)) ix[nb--] = n;                  \
+        else ix[nn++] = n;                                                           \
+      }                                                                              \
+      if (nn > 0) oqi_##SYM(row, ix, 0, nn - 1);                                     \
+      for (int64_t n = 0; n < N; n++) b[n * ib] = ix[n];                             \
+    }                                                                                \
+    free(row);                                                                       \
+    free(ix);                                                                        \
+  }                                                                                  \
+  /* Ufunc.pd:857-884: the average of the two middle elements for an even count */ \
+  static void medover_##SYM(octx *c, const int64_t *offs, int64_t n0, const int64_t *inc0) { \
+    int64_t N = c->ind_sizes[0], ia = c->inc_sizes[0][0];                            \
+    T *tmp = (T *)malloc(sizeof(T) * (N ? N : 1));                                   \
+    for (int64_t i0 = 0; i0 < n0; i0++) {                                            \
+      const T *a = (const T *)c->base[0] + offs[0] + i0 * inc0[0];                   \
+      T *b = (T *)c->base[1] + offs[1] + i0 * inc0[1];                               \
+      int64_t nn = sr_copy_##SYM(c, a, N, ia, tmp);                                  \
+      if (nn == 0) { *b = c->bad[1].SYM; continue; }                                 \
+      nn -= 1;                                                                       \
+      oq_##SYM(tmp, 0, nn);                                                          \
+      int64_t nn1 = nn / 2, nn2 = nn1 + 1;                                           \
+      if (nn % 2 == 0) *b = tmp[nn1];                                                \
+      else *b = (T)(0.5 * (tmp[nn1] + tmp[nn2]));                                    \
+    }                                                                                \
+    free(tmp);                                                                       \
+  }                                                                                  \
+  static void oddmedover_##SYM(octx *c, const int64_t *offs, int64_t n0, const int64_t *inc0) { \
+    int64_t N = c->ind_sizes[0], ia = c->inc_sizes[0][0];                            \
+    T *tmp = (T *)malloc(sizeof(T) * (N ? N : 1));                                   \
+    for (int64_t i0 = 0; i0 < n0; i0++) {                                            \
+      const T *a = (const T *)c->base[0] + offs[0] + i0 * inc0[0];                   \
+      T *b = (T *)c->base[1] + offs[1] + i0 * inc0[1];                               \
+      int64_t nn = sr_copy_##SYM(c, a, N, ia, tmp);                                  \
+      if (nn == 0) { *b = c->bad[1].SYM; continue; }                                 \
+      nn -= 1;                                                                       \
+      oq_##SYM(tmp, 0, nn);                                                          \
+      *b = tmp[nn / 2];                                                              \
+    }                                                                                \
+    free(tmp);                                                                       \
+  }                                                                                  \
+  /* Ufunc.pd:941-973: interpolated percentile, p clipped to [0, 1] */             \
+  static void pctover_##SYM(octx *c, const int64_t *offs, int64_t n0, const int64_t *inc0) { \
+    int64_t N = c->ind_sizes[0], ia = c->inc_sizes[0][0];                            \
+    T *tmp = (T *)malloc(sizeof(T) * (N ? N : 1));                                   \
+    for (int64_t i0 = 0; i0 < n0; i0++) {                                            \
+      const T *a = (const T *)c->base[0] + offs[0] + i0 * inc0[0];                   \
+      T p = *((const T *)c->base[1] + offs[1] + i0 * inc0[1]);                       \
+      T *b = (T *)c->base[2] + offs[2] + i0 * inc0[2];                               \
+      int64_t nn = sr_copy_##SYM(c, a, N, ia, tmp);                                  \
+      if (nn == 0) { *b = c->bad[2].SYM; continue; }                                 \
+      nn -= 1;                                                                       \
+      oq_##SYM(tmp, 0, nn);                                                          \
+      double np = nn * p, pp1, pp2;                                                  \
+      int64_t nn1 = (int64_t)(nn < (0 > np ? 0 : np) ? nn : (0 > np ? 0 : np));      \
+      int64_t nn2 = (int64_t)(nn < (0 > np + 1 ? 0 : np + 1) ? nn : (0 > np + 1 ? 0 : np + 1)); \
+      if (nn == 0) { pp1 = 0; pp2 = 0; }                                             \
+      else { pp1 = (double)nn1 / (double)nn; pp2 = (double)nn2 / (double)nn; }       \
+      if (np <= 0.0) *b = tmp[0];                                                    \
+      else if (np >= nn) *b = tmp[nn];                                               \
+      else if (tmp[nn2] == tmp[nn1]) *b = tmp[nn1];                                  \
+      else if (p == pp1) *b = tmp[nn1];                                              \
+      else if (p == pp2) *b = tmp[nn2];                                              \
+      else *b = (T)((np - nn1) * (tmp[nn2] - tmp[nn1]) + tmp[nn1]);                  \
+    }                                                                                \
+    free(tmp);                                                                       \
+  }                                                                                  \
+  /* Ufunc.pd:991-1005: the nearest data value */                                  \
+  static void oddpctover_##SYM(octx *c, const int64_t *offs, int64_t n0, const int64_t *inc0) { \
+    int64_t N = c->ind_sizes[0], ia = c->inc_sizes[0][0];                            \
+    T *tmp = (T *)malloc(sizeof(T) * (N ? N : 1));                                   \
+    for (int64_t i0 = 0; i0 < n0; i0++) {                                            \
+      const T *a = (const T *)c->base[0] + offs[0] + i0 * inc0[0];                   \
+      T p = *((const T *)c->base[1] + offs[1] + i0 * inc0[1]);                       \
+      T *b = (T *)c->base[2] + offs[2] + i0 * inc0[2];                               \
+      int64_t nn = sr_copy_##SYM(c, a, N, ia, tmp);                                  \
+      if (nn == 0) { *b = c->bad[2].SYM; continue; }                                 \
+      nn -= 1;                                                                       \
+      oq_##SYM(tmp, 0, nn);                                                          \
+      int64_t np = (int64_t)(0 > (nn < (nn + 1) * p ? nn : (nn + 1) * p)             \
+                                 ? 0 : (nn < (nn + 1) * p ? nn : (nn + 1) * p));      \
+      *b = tmp[np];                                                                  \
+    }                                                                                \
+    free(tmp);                                                                       \
+  }
+#define DEF_SORTREDS(E, CT, SYM, IP, ISF, UNS) DEF_SORTRED(CT, SYM, ISF, UNS)
+O_REAL_TYPES(DEF_SORTREDS)
+
+/* Ufunc.pd:905-939: the most frequent value of the sorted row (a value must
+ * repeat to count; bad values are values like any other) */
+#define DEF_MODEOVER(T, SYM)                                                         \
+  static void modeover_##SYM(octx *c, const int64_t *offs, int64_t n0, const int64_t *inc0) { \
+    int64_t N = c->ind_sizes[0], ia = c->inc_sizes[0][0];                            \
+    T *tmp = (T *)malloc(sizeof(T) * (N ? N : 1));                                   \
+    for (int64_t i0 = 0; i0 < n0; i0++) {                                            \
+      const T *a = (const T *)c->base[0] + offs[0] + i0 * inc0[0];                   \
+      T *o = (T *)c->base[1] + offs[1] + i0 * inc0[1];                               \
+      for (int64_t n = 0; n < N; n++) tmp[n] = a[n * ia];                            \
+      if (N > 0) oq_##SYM(tmp, 0, N - 1);                                            \
+      int64_t i = 0, most = 0;                                                       \
+      T curmode = 0, curval = 0;                                                     \
+      for (int64_t n = 0; n < N; n++) {                                              \
+        if (n == 0 || curval != tmp[n]) { curval = tmp[n]; i = 0; }                  \
+        else { i++; if (i > most) { most = i; curmode = curval; } }                  \
+      }                                                                              \
+      *o = curmode;                                                                  \
+    }                                                                                \
+    free(tmp);                                                                       \
+  }
+#define DEF_MODEOVERS(E, CT, SYM, IP, ISF, UNS) DEF_MODEOVER(CT, SYM)
+O_INT_TYPES(DEF_MODEOVERS)
+#define modeover_F NULL
+#define modeover_D NULL
+
 static body_fn pick_body(int op, int t) {
 #define CASE(OPID, PFX)                                                   \
   case OPID:                                                               \
@@ -952,6 +1163,13 @@ static body_fn pick_body(int op, int t) {
     CASE(OP_CUMUPRODOVER, cumuprodover)
     CASE(OP_DCUMUPRODOVER, dcumuprodover)
     CASE(OP_MINMAXIMUM, minmaximum)
+    CASE(OP_QSORT, qsort)
+    CASE(OP_QSORTI, qsorti)
+    CASE(OP_MEDOVER, medover)
+    CASE(OP_ODDMEDOVER, oddmedover)
+    CASE(OP_PCTOVER, pctover)
+    CASE(OP_ODDPCTOVER, oddpctover)
+    CASE(OP_MODEOVER, modeover)
   }
 #undef CASE
   return NULL;
@@ -1145,6 +1363,12 @@ int oracle_run(const char *opname, pdlgb300_ndarray **pdls_in, const int64_t *ot
   for (int k = 0; k < 3; k++) c.ind_sizes[k] = b.ind_sizes[k];
   body_fn fn = pick_body(op, tt);
   if (!fn) return set_err(&e, "no body for %s type %d", d->name, tt);
+  if (op == OP_MEDOVER || op == OP_ODDMEDOVER || op == OP_PCTOVER || op == OP_ODDPCTOVER) {
+    /* Ufunc.pd:857-858, $copy_to_temp: $CROAK("cannot process empty ndarray") */
+    int64_t nv = 1;
+    for (int k = 0; k < pdls[0]->ndims; k++) nv *= pdls[0]->dims[k];
+    if (nv == 0) return set_err(&e, "Error in %s:cannot process empty ndarray", d->name);
+  }
 
   int64_t maxvals = 0;
   for (int j = 0; j < d->npdls; j++) {

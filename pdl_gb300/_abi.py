@@ -95,6 +95,13 @@ SIGNATURES = {
     "pdlgb300_run_maximum": (Error, [P, P]),
     "pdlgb300_run_minimum_ind": (Error, [P, P]),
     "pdlgb300_run_minmaximum": (Error, [P, P, P, P, P]),
+    "pdlgb300_run_qsort": (Error, [P, P]),
+    "pdlgb300_run_qsorti": (Error, [P, P]),
+    "pdlgb300_run_medover": (Error, [P, P]),
+    "pdlgb300_run_oddmedover": (Error, [P, P]),
+    "pdlgb300_run_pctover": (Error, [P, P, P]),
+    "pdlgb300_run_oddpctover": (Error, [P, P, P]),
+    "pdlgb300_run_modeover": (Error, [P, P]),
     "pdlgb300_run_expr_reduce": (Error, [C.POINTER(Vtable), C.c_int32, PP, C.c_int32, C.c_void_p, P]),
     **{f"pdlgb300_run_{op}": (Error, [P, P])
        for op in ("andover", "orover", "xorover", "zcover", "bandover", "borover",

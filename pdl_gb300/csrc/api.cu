@@ -118,7 +118,8 @@ enum OpId {
   O_MINUS, O_DIVIDE, O_GT, O_LT, O_LE, O_GE, O_EQ, O_NE,
   O_SHIFTLEFT, O_SHIFTRIGHT, O_OR2, O_AND2, O_XOR,
   O_ANDOVER, O_OROVER, O_XOROVER, O_ZCOVER, O_BANDOVER, O_BOROVER, O_BXOROVER,
-  O_FIRSTNONZEROOVER, O_CUMUPRODOVER, O_DCUMUPRODOVER, O_MINMAXIMUM, O_NOPS
+  O_FIRSTNONZEROOVER, O_CUMUPRODOVER, O_DCUMUPRODOVER, O_MINMAXIMUM,
+  O_QSORT, O_QSORTI, O_MEDOVER, O_ODDMEDOVER, O_PCTOVER, O_ODDPCTOVER, O_MODEOVER, O_NOPS
 };
 
 // binary ops (a(); b(); [o]c(); int swap) and their kernel codes
@@ -153,6 +154,9 @@ const char *const N_ABDC[] = {"a", "b", "d", "c"};
 const char *const I_N[] = {"n"};
 const char *const N_MM4[] = {"a", "cmin", "cmax", "cmin_ind", "cmax_ind"};
 const char *const I_THW[] = {"t", "h", "w"};
+const char *const N_AI[] = {"a", "indx"};
+const char *const N_APB[] = {"a", "p", "b"};
+const char *const N_DO[] = {"data", "out"};
 
 const int32_t RD_10[] = {1, 0}, RD_11[] = {1, 1}, RD_000[] = {0, 0, 0},
               RD_110[] = {1, 1, 0}, RD_222[] = {2, 2, 2}, RD_1110[] = {1, 1, 1, 0};
@@ -163,6 +167,7 @@ const int32_t PT_L[] = {-1, PDLGB300_L}, PT_D[] = {-1, PDLGB300_D},
               PT_SMP[] = {-1, -1, -1, PDLGB300_L};
 const int32_t RD_10000[] = {1, 0, 0, 0, 0}, F_MM4[] = {0, OUT_C, OUT_C, OUT_T, OUT_T},
               PT_MM4[] = {-1, -1, -1, PDLGB300_IND, PDLGB300_IND};
+const int32_t RD_100[] = {1, 0, 0}, F_APB[] = {0, 0, OUT_C};
 const int32_t ID_N0[] = {0}, ID_NN[] = {0, 0}, ID_NNN[] = {0, 0, 0},
               ID_MM[] = {0, 1, 2, 0, 2, 1}, ID_NONE[] = {0};
 
@@ -211,6 +216,15 @@ const pdlgb300_vtable VT[O_NOPS] = {
     {"dcumuprodover", 2, 1, 1, 0, N_AB, RD_11, F_T, PT_D, ID_NN, I_N, REALTYPES},
     // lib/PDL/Ufunc.pd:563-613
     {"minmaximum", 5, 1, 1, 0, N_MM4, RD_10000, F_MM4, PT_MM4, ID_N0, I_N, REALTYPES},
+    // lib/PDL/Ufunc.pd:878-1112: the sort-based functions (real types;
+    // modeover the integer types)
+    {"qsort", 2, 1, 1, 0, N_AB, RD_11, F_C, PT_NONE, ID_NN, I_N, REALTYPES},
+    {"qsorti", 2, 1, 1, 0, N_AI, RD_11, F_T, PT_N, ID_NN, I_N, REALTYPES},
+    {"medover", 2, 1, 1, 0, N_AB, RD_10, F_C, PT_NONE, ID_N0, I_N, REALTYPES},
+    {"oddmedover", 2, 1, 1, 0, N_AB, RD_10, F_C, PT_NONE, ID_N0, I_N, REALTYPES},
+    {"pctover", 3, 2, 1, 0, N_APB, RD_100, F_APB, PT_NONE, ID_NNN, I_N, REALTYPES},
+    {"oddpctover", 3, 2, 1, 0, N_APB, RD_100, F_APB, PT_NONE, ID_NNN, I_N, REALTYPES},
+    {"modeover", 2, 1, 1, 0, N_DO, RD_10, F_C, PT_NONE, ID_N0, I_N, INTTYPES},
 };
 
 int op_of(const pdlgb300_vtable *vt) {
@@ -1151,6 +1165,59 @@ pdlgb300_error dispatch_minmaximum(RunCtx &c) {
   return launch_minmaximum(c.v[0].datatype, g, g_stream);
 }
 
+pdlgb300_error dispatch_sortred(RunCtx &c, int kind) {
+  const Brc &b = c.b;
+  SortArgs g;
+  memset(&g, 0, sizeof g);
+  const bool pct = kind == SR_PCT || kind == SR_ODDPCT;
+  const int np = pct ? 3 : 2;
+  const int which[3] = {0, 1, 2};
+  g.L = collapse(b, np, which);
+  g.out_pdl = np - 1;
+  g.rows = g.L.total;
+  g.n = b.ind_sizes[0];
+  g.inc_a = g.n <= 1 ? 1 : b.inc_sizes[0][0];
+  g.inc_b = (kind == SR_QSORT || kind == SR_QSORTI) && g.n > 1 ? b.inc_sizes[1][0] : 1;
+  g.a = c.dev[0];
+  g.p = pct ? c.dev[1] : nullptr;
+  g.b = c.dev[np - 1];
+  g.bad = c.bvalflag;
+  g.abad = bad_bits(&c.v[0]);
+  g.abad_isnan = bad_isnan(&c.v[0]);
+  g.obad = bad_bits(&c.v[np - 1]);
+  const int dt = c.v[0].datatype;
+  tl_info.rows = g.rows;
+  tl_info.n = g.n;
+  tl_info.bytes = (double)g.rows * g.n * TSIZES[dt] +
+                  (double)g.rows * (kind <= SR_QSORTI ? g.n : 1) * TSIZES[c.v[np - 1].datatype];
+  if (kind != SR_QSORT && kind != SR_QSORTI && kind != SR_MODE && nvals(&c.v[0]) == 0)
+    return err(PDLGB300_EUSERERROR, "Error in %s:cannot process empty ndarray", c.vt->name);
+  if (g.rows == 0 || g.n == 0) return ok();
+  void *scratch = nullptr;
+  const size_t vbytes = ((size_t)g.rows * g.n * TSIZES[dt] + 15) & ~(size_t)15;
+  const size_t ibytes = kind == SR_QSORTI ? (size_t)g.rows * g.n * sizeof(int64_t) : 0;
+  RET_IF(dalloc(vbytes + ibytes, &scratch));
+  g.scratch = scratch;
+  g.iscratch = ibytes ? (int64_t *)((char *)scratch + vbytes) : nullptr;
+  int *w = nullptr;
+  pdlgb300_error e = status_word(&w);
+  g.err = w;
+  int hs = 0;
+  if (!e.error) {
+    cudaError_t ce = cudaMemsetAsync(w, 0, sizeof(int), g_stream);
+    if (ce != cudaSuccess) e = err(PDLGB300_EFATAL, "clearing the status word: %s", cudaGetErrorString(ce));
+  }
+  if (!e.error) e = launch_sortred(kind, dt, g, g_stream);
+  if (!e.error) {
+    cudaError_t ce = cudaMemcpyAsync(&hs, w, sizeof(int), cudaMemcpyDeviceToHost, g_stream);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(g_stream);
+    if (ce != cudaSuccess) e = err(PDLGB300_EFATAL, "%s: %s", c.vt->name, cudaGetErrorString(ce));
+  }
+  cudaFreeAsync(scratch, g_stream);
+  if (!e.error && hs) e = err(PDLGB300_EFATAL, "%s: a sort scan left its range", c.vt->name);
+  return e;
+}
+
 pdlgb300_error dispatch_biop(RunCtx &c, int which_op) {
   BiopArgs g;
   memset(&g, 0, sizeof g);
@@ -1337,6 +1404,13 @@ pdlgb300_error dispatch(RunCtx &c, const int64_t *) {
     case O_BXOROVER: return dispatch_reduce(c, R_BXOR);
     case O_FIRSTNONZEROOVER: return dispatch_reduce(c, R_FIRSTNZ);
     case O_MINMAXIMUM: return dispatch_minmaximum(c);
+    case O_QSORT: return dispatch_sortred(c, SR_QSORT);
+    case O_QSORTI: return dispatch_sortred(c, SR_QSORTI);
+    case O_MEDOVER: return dispatch_sortred(c, SR_MED);
+    case O_ODDMEDOVER: return dispatch_sortred(c, SR_ODDMED);
+    case O_PCTOVER: return dispatch_sortred(c, SR_PCT);
+    case O_ODDPCTOVER: return dispatch_sortred(c, SR_ODDPCT);
+    case O_MODEOVER: return dispatch_sortred(c, SR_MODE);
     case O_CUMUPRODOVER: return dispatch_cumusum(c, 2);
     case O_DCUMUPRODOVER: return dispatch_cumusum(c, 3);
     case O_INNER: return dispatch_inner(c);
@@ -1751,6 +1825,21 @@ RUN2(bxorover, O_BXOROVER)
 RUN2(firstnonzeroover, O_FIRSTNONZEROOVER)
 RUN2(cumuprodover, O_CUMUPRODOVER)
 RUN2(dcumuprodover, O_DCUMUPRODOVER)
+RUN2(qsort, O_QSORT)
+RUN2(qsorti, O_QSORTI)
+RUN2(medover, O_MEDOVER)
+RUN2(oddmedover, O_ODDMEDOVER)
+RUN2(modeover, O_MODEOVER)
+
+pdlgb300_error pdlgb300_run_pctover(pdlgb300_ndarray *a, pdlgb300_ndarray *p, pdlgb300_ndarray *b) {
+  pdlgb300_ndarray *q[3] = {a, p, b};
+  return guard_run(O_PCTOVER, q, nullptr);
+}
+pdlgb300_error pdlgb300_run_oddpctover(pdlgb300_ndarray *a, pdlgb300_ndarray *p,
+                                       pdlgb300_ndarray *b) {
+  pdlgb300_ndarray *q[3] = {a, p, b};
+  return guard_run(O_ODDPCTOVER, q, nullptr);
+}
 
 pdlgb300_error pdlgb300_run_minmaximum(pdlgb300_ndarray *a, pdlgb300_ndarray *cmin,
                                        pdlgb300_ndarray *cmax, pdlgb300_ndarray *cmin_ind,

@@ -119,6 +119,24 @@ struct MM4Args {
 };
 pdlgb300_error launch_minmaximum(int dt, const MM4Args &g, cudaStream_t s);
 
+// The sort-based functions of PDL::Ufunc (sortred.cu).
+enum SortKind { SR_QSORT, SR_QSORTI, SR_MED, SR_ODDMED, SR_PCT, SR_ODDPCT, SR_MODE };
+struct SortArgs {
+  const char *a;      // element (0) of a
+  const char *p;      // element (0) of p (pctover, oddpctover)
+  char *b;            // element (0) of the output
+  int out_pdl;        // the output's index in L
+  int64_t n, inc_a, inc_b, rows;
+  Loop L;             // pdl 0 a, [1 p], then the output
+  int bad;
+  uint64_t abad, obad;
+  int abad_isnan;
+  void *scratch;      // rows x n elements: each row's private copy
+  int64_t *iscratch;  // rows x n indices (qsorti)
+  int *err;           // bit 0: a scan left its range (never expected)
+};
+pdlgb300_error launch_sortred(int kind, int dt, const SortArgs &g, cudaStream_t s);
+
 struct ConvArgs {
   const char *src;
   char *dst;

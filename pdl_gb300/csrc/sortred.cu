@@ -1,0 +1,256 @@
+// sortred.cu -- the sort-based functions of PDL::Ufunc over dim 0
+// (lib/PDL/Ufunc.pd:744-1115): qsort, qsorti, medover, oddmedover, pctover,
+// oddpctover, modeover.
+//
+// The reference sorts with its own quicksort (lib/PDL/Core/pdl.h.PL:618-640
+// for values, Ufunc.pd:745-767 for indices: the middle element as pivot,
+// the two scans, swap, then the ranges [a,j] and [i,b]).  Its results are
+// not those of every sort: the order of equal keys in qsorti, the placement
+// of NaN, and which of -0 and +0 comes first all follow from the steps it
+// takes.  So each row runs the same steps here, one thread per row over a
+// private copy of the row in device scratch: the results are the
+// reference's in every case.  The two ranges after a partition are
+// disjoint, so sorting the smaller one first (an explicit stack, at most
+// 64 entries) and continuing with the larger one gives the same array.
+// Scans are bounded by their range (they cannot leave it: the pivot and the
+// elements swapped behind the scans stop them); a violation sets an error
+// bit and ends the row.
+#include "args.cuh"
+
+namespace pg {
+namespace {
+
+constexpr int QS_STACK = 64;
+
+template <class T>
+__device__ bool qs_values(T *xx, int64_t a, int64_t b) {
+  int64_t st[2 * QS_STACK];
+  int sp = 0;
+  for (;;) {
+    while (a < b) {
+      int64_t i = a, j = b;
+      const T median = xx[(i + j) / 2];
+      do {
+        while (xx[i] < median) {
+          if (++i > b) return false;
+        }
+        while (median < xx[j]) {
+          if (--j < a) return false;
+        }
+        if (i <= j) {
+          const T t = xx[i];
+          xx[i] = xx[j];
+          xx[j] = t;
+          i++;
+          j--;
+        }
+      } while (i <= j);
+      // [a, j] and [i, b]: push the larger, continue with the smaller
+      int64_t la = a, lb = j, ra = i, rb = b;
+      if (j - a > b - i) {
+        la = i; lb = b; ra = a; rb = j;
+      }
+      if (ra < rb) {
+        if (sp >= QS_STACK) return false;
+        st[2 * sp] = ra;
+        st[2 * sp + 1] = rb;
+        sp++;
+      }
+      a = la;
+      b = lb;
+    }
+    if (sp == 0) return true;
+    sp--;
+    a = st[2 * sp];
+    b = st[2 * sp + 1];
+  }
+}
+
+template <class T>
+__device__ bool qs_indices(const T *xx, int64_t *ix, int64_t a, int64_t b) {
+  int64_t st[2 * QS_STACK];
+  int sp = 0;
+  for (;;) {
+    while (a < b) {
+      int64_t i = a, j = b;
+      const T median = xx[ix[(i + j) / 2]];
+      do {
+        while (xx[ix[i]] < median) {
+          if (++i > b) return false;
+        }
+        while (median < xx[ix[j]]) {
+          if (--j < a) return false;
+        }
+        if (i <= j) {
+          const int64_t t = ix[i];
+          ix[i] = ix[j];
+          ix[j] = t;
+          i++;
+          j--;
+        }
+      } while (i <= j);
+      int64_t la = a, lb = j, ra = i, rb = b;
+      if (j - a > b - i) {
+        la = i; lb = b; ra = a; rb = j;
+      }
+      if (ra < rb) {
+        if (sp >= QS_STACK) return false;
+        st[2 * sp] = ra;
+        st[2 * sp + 1] = rb;
+        sp++;
+      }
+      a = la;
+      b = lb;
+    }
+    if (sp == 0) return true;
+    sp--;
+    a = st[2 * sp];
+    b = st[2 * sp + 1];
+  }
+}
+
+// 0.5 * (x + y) in the reference's C: the sum in the promoted type
+// (integers wrap), the product in double, then back to T.
+template <class T> __device__ __forceinline__ T half_sum(T x, T y) {
+  if constexpr (std::is_floating_point_v<T>) {
+    return (T)(0.5 * (double)(x + y));
+  } else {
+    using P = decltype(x + y);
+    using U = std::make_unsigned_t<P>;
+    const P s = (P)(U)((U)(P)x + (U)(P)y);
+    return (T)(0.5 * (double)s);
+  }
+}
+
+template <class T, int K, bool BAD>
+__global__ void __launch_bounds__(128) k_sortred(const SortArgs g) {
+  const Bad<T> bv{from_bits<T>(g.abad), (bool)g.abad_isnan};
+  const T obad = from_bits<T>(g.obad);
+  for (int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; row < g.rows;
+       row += (int64_t)gridDim.x * blockDim.x) {
+    int64_t offs[MAXP];
+    loop_offsets(g.L, row, offs);
+    const T *a = reinterpret_cast<const T *>(g.a) + offs[0];
+    T *tmp = reinterpret_cast<T *>(g.scratch) + row * g.n;
+    const int ob = g.out_pdl;
+    if constexpr (K == SR_QSORTI) {
+      int64_t *ix = g.iscratch + row * g.n;
+      int64_t *out = reinterpret_cast<int64_t *>(g.b) + offs[ob];
+      int64_t nn = 0, nb = g.n - 1;
+      for (int64_t t = 0; t < g.n; t++) {
+        const T v = a[t * g.inc_a];
+        tmp[t] = v;
+        if (BAD && bv.is(v)) ix[nb--] = t;
+        else ix[nn++] = t;
+      }
+      if (nn > 0 && !qs_indices<T>(tmp, ix, 0, nn - 1)) atomicOr(g.err, 1);
+      for (int64_t t = 0; t < g.n; t++) out[t * g.inc_b] = ix[t];
+      continue;
+    }
+    // the good elements (all of them for modeover, which has no bad rule)
+    int64_t nn = 0;
+    for (int64_t t = 0; t < g.n; t++) {
+      const T v = a[t * g.inc_a];
+      if (K != SR_MODE && BAD && bv.is(v)) continue;
+      tmp[nn++] = v;
+    }
+    T *out = reinterpret_cast<T *>(g.b) + offs[ob];
+    if (nn > 0 && !qs_values<T>(tmp, 0, nn - 1)) atomicOr(g.err, 1);
+    if constexpr (K == SR_QSORT) {
+      for (int64_t t = 0; t < g.n; t++) out[t * g.inc_b] = t < nn ? tmp[t] : obad;
+      continue;
+    }
+    if constexpr (K == SR_MODE) {
+      int64_t i = 0, most = 0;
+      T curmode = 0, curval = 0;
+      for (int64_t t = 0; t < nn; t++) {
+        if (t == 0 || curval != tmp[t]) {
+          curval = tmp[t];
+          i = 0;
+        } else if (++i > most) {
+          most = i;
+          curmode = curval;
+        }
+      }
+      *out = curmode;
+      continue;
+    }
+    if (nn == 0) {
+      *out = obad;  // a row with no good element (bad-value mode only)
+      continue;
+    }
+    const int64_t last = nn - 1;
+    if constexpr (K == SR_MED) {
+      const int64_t n1 = last / 2;
+      *out = last % 2 == 0 ? tmp[n1] : half_sum<T>(tmp[n1], tmp[n1 + 1]);
+    } else if constexpr (K == SR_ODDMED) {
+      *out = tmp[last / 2];
+    } else if constexpr (K == SR_PCT) {
+      const T p = *(reinterpret_cast<const T *>(g.p) + offs[1]);
+      // the reference's mixed-type arithmetic, step by step
+      const double np = last * p;
+      const double lo0 = 0 > np ? 0 : np, lo1 = 0 > np + 1 ? 0 : np + 1;
+      const int64_t n1 = (int64_t)(last < lo0 ? (double)last : lo0);
+      const int64_t n2 = (int64_t)(last < lo1 ? (double)last : lo1);
+      double pp1 = 0, pp2 = 0;
+      if (last != 0) {
+        pp1 = (double)n1 / (double)last;
+        pp2 = (double)n2 / (double)last;
+      }
+      T r;
+      if (np <= 0.0) r = tmp[0];
+      else if (np >= last) r = tmp[last];
+      else if (tmp[n2] == tmp[n1]) r = tmp[n1];
+      else if (p == pp1) r = tmp[n1];
+      else if (p == pp2) r = tmp[n2];
+      else  // no contraction into a fused multiply-add, as in the reference's C
+        r = (T)__dadd_rn(__dmul_rn(np - (double)n1, (double)(tmp[n2] - tmp[n1])),
+                         (double)tmp[n1]);
+      *out = r;
+    } else {  // SR_ODDPCT
+      const T p = *(reinterpret_cast<const T *>(g.p) + offs[1]);
+      const auto q = (last + 1) * p;
+      const auto m = last < q ? (decltype(q))last : q;
+      const int64_t np = (int64_t)(0 > m ? (decltype(q))0 : m);
+      *out = tmp[np];
+    }
+  }
+}
+
+template <class T, int K>
+pdlgb300_error go_sort(const SortArgs &g, cudaStream_t s) {
+  pdlgb300_error e = pgh::ok();
+  const int nsm = pgh::num_sms();
+  const int64_t grid = std::max<int64_t>(1, std::min<int64_t>((g.rows + 127) / 128, (int64_t)nsm * 16));
+  if (g.bad) k_sortred<T, K, true><<<(int)grid, 128, 0, s>>>(g);
+  else k_sortred<T, K, false><<<(int)grid, 128, 0, s>>>(g);
+  if (!pgh::cuda_check(cudaGetLastError(), &e, "k_sortred")) return e;
+  pgh::record_kernel("k_sortred", grid, 128);
+  return e;
+}
+
+template <int DT>
+pdlgb300_error sort_family(int k, const SortArgs &g, cudaStream_t s) {
+  using T = typename TT<DT>::T;
+  switch (k) {
+    case SR_QSORT: return go_sort<T, SR_QSORT>(g, s);
+    case SR_QSORTI: return go_sort<T, SR_QSORTI>(g, s);
+    case SR_MED: return go_sort<T, SR_MED>(g, s);
+    case SR_ODDMED: return go_sort<T, SR_ODDMED>(g, s);
+    case SR_PCT: return go_sort<T, SR_PCT>(g, s);
+    case SR_ODDPCT: return go_sort<T, SR_ODDPCT>(g, s);
+    case SR_MODE:
+      if constexpr (std::is_integral_v<T>) return go_sort<T, SR_MODE>(g, s);
+      break;
+  }
+  return pgh::err(PDLGB300_EUSERERROR, "sort-based function %d: unsupported type %d", k, DT);
+}
+
+}  // namespace
+
+pdlgb300_error launch_sortred(int k, int dt, const SortArgs &g, cudaStream_t s) {
+  PG_DISPATCH(dt, return sort_family<DT>(k, g, s));
+  return pgh::err(PDLGB300_EUSERERROR, "sort-based function: unsupported type %d", dt);
+}
+
+}  // namespace pg

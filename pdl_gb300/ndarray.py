@@ -359,6 +359,18 @@ class ndarray:
     def maximum_ind(self, out=None): return maximum_ind(self, out)
     def inner(self, o, out=None): return inner(self, o, out)
     def minmaximum(self): return minmaximum(self)
+    def qsort(self, out=None): return qsort(self, out)
+    def qsorti(self, out=None): return qsorti(self, out)
+    def medover(self, out=None): return medover(self, out)
+    def oddmedover(self, out=None): return oddmedover(self, out)
+    def modeover(self, out=None): return modeover(self, out)
+    def pctover(self, p, out=None): return pctover(self, p, out)
+    def oddpctover(self, p, out=None): return oddpctover(self, p, out)
+    def median(self): return self.flat().medover()
+    def oddmedian(self): return self.flat().oddmedover()
+    def mode(self): return self.flat().modeover()
+    def pct(self, p): return pctover(self.flat(), p)
+    def oddpct(self, p): return oddpctover(self.flat(), p)
 
     # whole-array reductions (lib/PDL/Ufunc.pd:615-663): flat, then the
     # reduction over dim 0
@@ -582,6 +594,27 @@ def minmaximum(a, cmin=None, cmax=None, cmin_ind=None, cmax_ind=None):
 
 
 minmaxover = minmaximum
+qsort = _red("qsort")
+qsorti = _red("qsorti")
+medover = _red("medover")
+oddmedover = _red("oddmedover")
+modeover = _red("modeover")
+
+
+def pctover(a, p, out=None) -> "ndarray":
+    """The p-th percentile over dim 0, interpolated (lib/PDL/Ufunc.pd:975-989)."""
+    a = _scalar_to_pdl(a, None)
+    p = _scalar_to_pdl(p, a)
+    o = None if out is None or isinstance(out, _Null) else out
+    return _run("pctover", [a, p], [o])[0]
+
+
+def oddpctover(a, p, out=None) -> "ndarray":
+    """The p-th percentile over dim 0, the nearest data value (Ufunc.pd:991-1007)."""
+    a = _scalar_to_pdl(a, None)
+    p = _scalar_to_pdl(p, a)
+    o = None if out is None or isinstance(out, _Null) else out
+    return _run("oddpctover", [a, p], [o])[0]
 dcumuprodover = _red("dcumuprodover")
 minimum_ind = _red("minimum_ind")
 maximum_ind = _red("maximum_ind")

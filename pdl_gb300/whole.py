@@ -2,7 +2,8 @@
 argument (clump(-1), a view where the strides allow) and runs the matching
 reduction over dim 0, returning a 0-dim ndarray.  and/or are keywords in
 Python, so those two are and_/or_; any/all alias or_/and_ as in the
-reference (Ufunc.pd:665-710)."""
+reference (Ufunc.pd:665-710).  median, oddmedian, mode, pct and oddpct are
+the sort-based ones (Ufunc.pd:615-663, 1009-1038)."""
 from .ndarray import _scalar_to_pdl
 
 
@@ -31,3 +32,16 @@ min = _whole("min")  # noqa: A001
 max = _whole("max")  # noqa: A001
 any = or_  # noqa: A001
 all = and_  # noqa: A001
+median = _whole("median")
+oddmedian = _whole("oddmedian")
+mode = _whole("mode")
+
+
+def pct(x, p):
+    """The p-th percentile of all elements, interpolated (Ufunc.pd:1009-1038)."""
+    return _scalar_to_pdl(x, None).pct(p)
+
+
+def oddpct(x, p):
+    """The p-th percentile of all elements, the nearest data value."""
+    return _scalar_to_pdl(x, None).oddpct(p)

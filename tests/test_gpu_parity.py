@@ -484,7 +484,7 @@ def _golden_gpu(case):
     if case.get("view") == "dim1_index1":
         ins[0] = ins[0].slice(slice(None), 1)
     if "whole" in case:
-        return getattr(P, case["whole"])(ins[0])
+        return getattr(P, case["whole"])(*ins)
     out = None
     if "out" in case:
         kind, dims = case["out"].split(":")
@@ -497,11 +497,14 @@ def _golden_gpu(case):
         return fn(*ins)[case.get("pick", 0)]
     if case["op"] in P_BIOPS:
         return fn(ins[0], ins[1], out, swap=case.get("swap", 0))
+    if case["op"] in P_TWO_IN:
+        return fn(ins[0], ins[1], out)
     return fn(*ins, out) if out is not None else fn(*ins)
 
 
 P_BIOPS = {"plus", "mult", "minus", "divide", "gt", "lt", "le", "ge", "eq", "ne",
            "shiftleft", "shiftright", "or2", "and2", "xor"}
+P_TWO_IN = {"pctover", "oddpctover"}
 
 
 def test_golden_vectors_on_the_gpu(gpu):
@@ -731,3 +734,90 @@ def test_whole_array_reductions(gpu, t):
                 assert_same(got, exp, atol=(n + 2) * eps * absum, what=f"{name} {t}")
             else:
                 assert_same(got, exp, what=f"{name} {t}")
+
+
+SORT_OPS = ["qsort", "qsorti", "medover", "oddmedover"]
+
+
+def _bits_equal(got, exp, what):
+    assert got.type == exp.type and got.dims == exp.dims, what
+    assert got.badflag() == exp.badflag(), what
+    g, e = got.numpy(), exp.numpy()
+    assert np.array_equal(g.view(np.uint8), e.view(np.uint8)), (
+        f"{what}: got {g.ravel()[:12]} exp {e.ravel()[:12]}")
+
+
+def _sort_data(rng, t, shape, bad_frac=0.0):
+    """Few distinct values (ties), and for floats NaN and both zeros."""
+    a, bad = rand_array(rng, t, shape, -4, 4, bad_frac=bad_frac)
+    dt = a.dtype
+    if dt.kind == "f":
+        a = np.round(a).astype(dt)
+        flat = a.reshape(-1)
+        k = max(1, flat.size // 20)
+        flat[rng.integers(0, flat.size, k)] = np.nan
+        flat[rng.integers(0, flat.size, k)] = -0.0
+        flat[rng.integers(0, flat.size, k)] = 0.0
+        if bad_frac:
+            a[bad] = P.default_badvalue(type_code(str(t)))
+    return a
+
+
+@pytest.mark.parametrize("t", REAL_TYPES)
+@pytest.mark.parametrize("op", SORT_OPS)
+def test_sort_based_bit_exact(gpu, op, t):
+    """Ufunc.pd:878-1112 against the oracle bit for bit: the GPU runs the
+    reference's quicksort steps, so ties (qsorti's index order), NaN
+    placement and the signs of zeros all agree; bad values, strided views."""
+    rng = seeded(("sort", op, t))
+    for shape in [(7,), (1,), (33, 17), (200, 40), (3, 1000)]:
+        x = to_pdl(_sort_data(rng, t, shape[::-1]), t)
+        got, exp = _run_both(op, [x])
+        _bits_equal(got, exp, f"{op} {t} {shape}")
+    a = _sort_data(rng, t, (12, 300), bad_frac=0.25)
+    a[0, :] = P.default_badvalue(type_code(t))
+    xb = to_pdl(a, t, badflag=True)
+    got, exp = _run_both(op, [xb])
+    _bits_equal(got, exp, f"{op} {t} bad")
+    v = to_pdl(_sort_data(rng, t, (20, 30, 5)), t).xchg(0, 1)
+    got, exp = _run_both(op, [v])
+    _bits_equal(got, exp, f"{op} {t} strided")
+
+
+@pytest.mark.parametrize("t", ["byte", "long", "longlong", "float", "double"])
+@pytest.mark.parametrize("op", ["pctover", "oddpctover"])
+def test_percentiles_bit_exact(gpu, op, t):
+    rng = seeded(("pct", op, t))
+    for n in [1, 2, 5, 25, 300]:
+        a = _sort_data(rng, t, (9, n))
+        x = to_pdl(a, t)
+        for p in [-0.5, 0.0, 0.1, 0.23, 0.5, 0.77, 0.9, 1.0, 2.0]:
+            pp = P.pdl(np.array(p))
+            got = getattr(P, op)(x, pp)
+            exp = O.run(op, [x, pp])[0]
+            _bits_equal(got, exp, f"{op} {t} n={n} p={p}")
+    # p broadcast per row, and bad values
+    a = _sort_data(rng, t, (16, 50), bad_frac=0.3)
+    x = to_pdl(a, t, badflag=True)
+    pp = P.pdl(rng.uniform(-0.2, 1.2, size=16))
+    _bits_equal(getattr(P, op)(x, pp), O.run(op, [x, pp])[0], f"{op} {t} per-row p")
+
+
+@pytest.mark.parametrize("t", ["sbyte", "byte", "short", "ushort", "long", "ulong", "longlong"])
+def test_modeover(gpu, t):
+    rng = seeded(("mode", t))
+    for shape in [(7,), (40, 33), (5, 1000)]:
+        a, _ = rand_array(rng, t, shape[::-1], 0, 6)
+        x = to_pdl(a, t)
+        got, exp = _run_both("modeover", [x])
+        _bits_equal(got, exp, f"modeover {t} {shape}")
+
+
+def test_sort_based_empty_and_errors(gpu):
+    with pytest.raises(P.PDLError, match="Error in medover:cannot process empty ndarray"):
+        P.medover(P.zeroes("double", 0))
+    with pytest.raises(P.PDLError, match="cannot process empty ndarray"):
+        P.pctover(P.zeroes("double", 0, 3), 0.5)
+    e = P.qsort(P.zeroes("double", 0))          # the reference returns at once
+    assert e.dims == (0,)
+    assert P.qsorti(P.pdl(np.array([8.0]))).numpy().tolist() == [0]

@@ -52,6 +52,14 @@ def check_result(case, got):
     exp_t = case.get("expect_type")
     if exp_t:
         assert got.type == exp_t
+    if case.get("check") == "index":
+        # the reference's test: the input indexed by the result is `expect`
+        src = make_input(case["inputs"][0])
+        vals = src.numpy().reshape(-1)[got.numpy().reshape(-1)]
+        e, bad = _parse_data(case["expect"], src.datatype)
+        assert np.array_equal(vals[~bad], e[~bad])
+        assert np.all(vals[bad] == P.default_badvalue(src.datatype))
+        return
     g = got.numpy()
     if "expect_badflag" in case:
         assert int(got.badflag()) == case["expect_badflag"]
