@@ -742,7 +742,14 @@ SORT_OPS = ["qsort", "qsorti", "medover", "oddmedover"]
 def _bits_equal(got, exp, what):
     assert got.type == exp.type and got.dims == exp.dims, what
     assert got.badflag() == exp.badflag(), what
-    g, e = got.numpy(), exp.numpy()
+    g, e = np.atleast_1d(got.numpy()), np.atleast_1d(exp.numpy())
+    if g.dtype.kind == "f":
+        # NaN produced by arithmetic has a hardware-defined payload (the
+        # GPU's canonical NaN, x86's default NaN): compare NaN positions,
+        # then every other element bit for bit (signed zeros included)
+        gn, en = np.isnan(g), np.isnan(e)
+        assert np.array_equal(gn, en), f"{what}: NaN positions differ"
+        g, e = np.where(gn, 0, g), np.where(en, 0, e)
     assert np.array_equal(g.view(np.uint8), e.view(np.uint8)), (
         f"{what}: got {g.ravel()[:12]} exp {e.ravel()[:12]}")
 
