@@ -271,6 +271,7 @@ def run_ours(args, rank, world):
         result["fused_c2"] = bench_c2(args, P, torch, stream)
         result["inner_c3"] = bench_inner(args, P, torch, stream, hbm)
         result["expr"] = bench_expr(args, P, torch, stream, hbm)
+        result["sort"] = bench_sort(args, P, torch, stream, hbm)
     if rank == 0 and not args.no_cpu:
         result["cpu_baseline"] = cpu_baseline(args, mat)
     return result
@@ -595,6 +596,36 @@ def bench_expr(args, P, torch, stream, hbm):
     return {"config": f"sumover((a-b)*(a-b)), float32 a,b dims (65536,{rows}) N(0,1) seed 8 -> {rows}",
             "ms": ms, "gbs": gbs, "frac_of_hbm": gbs / hbm, "op": op,
             "eager_ms": ms_eager, "speedup_vs_eager": ms_eager / ms}
+
+
+def bench_sort(args, P, torch, stream, hbm):
+    """Sort-based reductions: medover and qsorti over float32 dims (100, 65536)
+    (65536 rows of 100 values, N(0,1), seed 9: a per-pixel median of a
+    100-frame stack), the reference's quicksort per row on the GPU; the
+    oracle (the same quicksort in C, all host threads) on 8192 of the rows."""
+    from oracle import oracle as O
+    rng = np.random.default_rng(9)
+    a = rng.standard_normal((65536, 100), dtype=np.float32)
+    x = P.pdl(a).to_device()
+    out = {"config": "medover and qsorti, float32 dims (100, 65536) N(0,1) seed 9"}
+    nbytes = 65536 * 100 * 4
+    for op in ("medover", "qsorti"):
+        r = getattr(P, op)(x)
+        P.sync()
+        ms = time_op(torch, stream, lambda: getattr(P, op)(x), 5)
+        out[op] = {"ms": ms, "rows_per_s": 65536 / (ms * 1e-3), "gbs_in": nbytes / (ms * 1e-3) / 1e9,
+                   "kernel": "k_sortred"}
+        del r
+    xs = P.pdl(np.ascontiguousarray(a[:8192]))
+    n = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    O.run("medover", [xs], nthreads=n)
+    el = time.perf_counter() - t0
+    out["cpu_medover"] = {"rows_per_s": 8192 / el, "cores": n, "kind": "port",
+                          "sample": "8192 of the 65536 rows"}
+    out["bound"] = ("one thread per row running the reference's sequential quicksort "
+                    "(latency of its dependent loads), not HBM")
+    return out
 
 
 def cpu_time(mat, nrows, nthreads, budget_s, steps=None):
