@@ -66,8 +66,8 @@ __device__ bool qs_values(T *xx, int64_t a, int64_t b) {
   }
 }
 
-template <class T>
-__device__ bool qs_indices(const T *xx, int64_t *ix, int64_t a, int64_t b) {
+template <class T, class I>
+__device__ bool qs_indices(const T *xx, I *ix, int64_t a, int64_t b) {
   int64_t st[2 * QS_STACK];
   int sp = 0;
   for (;;) {
@@ -82,7 +82,7 @@ __device__ bool qs_indices(const T *xx, int64_t *ix, int64_t a, int64_t b) {
           if (--j < a) return false;
         }
         if (i <= j) {
-          const int64_t t = ix[i];
+          const I t = ix[i];
           ix[i] = ix[j];
           ix[j] = t;
           i++;
@@ -122,6 +122,74 @@ template <class T> __device__ __forceinline__ T half_sum(T x, T y) {
   }
 }
 
+// The outputs of a row from its sorted good values tmp[0, nn): qsort
+// writes all n (lanes `lane` of G in parallel), the others one value
+// (lane 0).
+template <class T, int K>
+__device__ __forceinline__ void finish_values(const SortArgs &g, const T *tmp, int64_t nn,
+                                              const int64_t *offs, T *out, T obad, int lane,
+                                              int G) {
+  if constexpr (K == SR_QSORT) {
+    for (int64_t t = lane; t < g.n; t += G) out[t * g.inc_b] = t < nn ? tmp[t] : obad;
+    return;
+  }
+  if (lane != 0) return;
+  if constexpr (K == SR_MODE) {
+    int64_t i = 0, most = 0;
+    T curmode = 0, curval = 0;
+    for (int64_t t = 0; t < nn; t++) {
+      if (t == 0 || curval != tmp[t]) {
+        curval = tmp[t];
+        i = 0;
+      } else if (++i > most) {
+        most = i;
+        curmode = curval;
+      }
+    }
+    *out = curmode;
+    return;
+  }
+  if (nn == 0) {
+    *out = obad;  // a row with no good element (bad-value mode only)
+    return;
+  }
+  const int64_t last = nn - 1;
+  if constexpr (K == SR_MED) {
+    const int64_t n1 = last / 2;
+    *out = last % 2 == 0 ? tmp[n1] : half_sum<T>(tmp[n1], tmp[n1 + 1]);
+  } else if constexpr (K == SR_ODDMED) {
+    *out = tmp[last / 2];
+  } else if constexpr (K == SR_PCT) {
+    const T p = *(reinterpret_cast<const T *>(g.p) + offs[1]);
+    // the reference's mixed-type arithmetic, step by step
+    const double np = last * p;
+    const double lo0 = 0 > np ? 0 : np, lo1 = 0 > np + 1 ? 0 : np + 1;
+    const int64_t n1 = (int64_t)(last < lo0 ? (double)last : lo0);
+    const int64_t n2 = (int64_t)(last < lo1 ? (double)last : lo1);
+    double pp1 = 0, pp2 = 0;
+    if (last != 0) {
+      pp1 = (double)n1 / (double)last;
+      pp2 = (double)n2 / (double)last;
+    }
+    T r;
+    if (np <= 0.0) r = tmp[0];
+    else if (np >= last) r = tmp[last];
+    else if (tmp[n2] == tmp[n1]) r = tmp[n1];
+    else if (p == pp1) r = tmp[n1];
+    else if (p == pp2) r = tmp[n2];
+    else  // no contraction into a fused multiply-add, as in the reference's C
+      r = (T)__dadd_rn(__dmul_rn(np - (double)n1, (double)(tmp[n2] - tmp[n1])),
+                       (double)tmp[n1]);
+    *out = r;
+  } else {  // SR_ODDPCT
+    const T p = *(reinterpret_cast<const T *>(g.p) + offs[1]);
+    const auto q = (last + 1) * p;
+    const auto m = last < q ? (decltype(q))last : q;
+    const int64_t np = (int64_t)(0 > m ? (decltype(q))0 : m);
+    *out = tmp[np];
+  }
+}
+
 template <class T, int K, bool BAD>
 __global__ void __launch_bounds__(128) k_sortred(const SortArgs g) {
   const Bad<T> bv{from_bits<T>(g.abad), (bool)g.abad_isnan};
@@ -143,7 +211,7 @@ __global__ void __launch_bounds__(128) k_sortred(const SortArgs g) {
         if (BAD && bv.is(v)) ix[nb--] = t;
         else ix[nn++] = t;
       }
-      if (nn > 0 && !qs_indices<T>(tmp, ix, 0, nn - 1)) atomicOr(g.err, 1);
+      if (nn > 0 && !qs_indices<T, int64_t>(tmp, ix, 0, nn - 1)) atomicOr(g.err, 1);
       for (int64_t t = 0; t < g.n; t++) out[t * g.inc_b] = ix[t];
       continue;
     }
@@ -156,64 +224,158 @@ __global__ void __launch_bounds__(128) k_sortred(const SortArgs g) {
     }
     T *out = reinterpret_cast<T *>(g.b) + offs[ob];
     if (nn > 0 && !qs_values<T>(tmp, 0, nn - 1)) atomicOr(g.err, 1);
-    if constexpr (K == SR_QSORT) {
-      for (int64_t t = 0; t < g.n; t++) out[t * g.inc_b] = t < nn ? tmp[t] : obad;
-      continue;
+    finish_values<T, K>(g, tmp, nn, offs, out, obad, 0, 1);
+  }
+}
+
+// Short rows (n <= SF_MAX): one warp per row over shared memory.  Where
+// the result cannot depend on how the row is sorted -- the good values
+// hold no NaN and not both -0 and +0 (for qsorti also no two equal
+// values) -- the warp sorts with a bitonic network (ties broken by
+// position, a total order); any other row is sorted by lane 0 with the
+// reference's quicksort over the same shared-memory copy, as in k_sortred.
+// The bad indices of qsorti are final when found: from the end backwards.
+constexpr int SF_MAX = 512, SF_WARPS = 4;
+
+template <class T> __device__ __forceinline__ bool sf_unsafe_float(T v, bool &neg0, bool &pos0) {
+  if constexpr (std::is_floating_point_v<T>) {
+    if (v != v) return true;
+    if (v == (T)0) {
+      if (signbit(v)) neg0 = true;
+      else pos0 = true;
     }
-    if constexpr (K == SR_MODE) {
-      int64_t i = 0, most = 0;
-      T curmode = 0, curval = 0;
-      for (int64_t t = 0; t < nn; t++) {
-        if (t == 0 || curval != tmp[t]) {
-          curval = tmp[t];
-          i = 0;
-        } else if (++i > most) {
-          most = i;
-          curmode = curval;
+  }
+  return false;
+}
+
+template <class T, int K, bool BAD>
+__global__ void __launch_bounds__(SF_WARPS * 32) k_sortred_warp(const SortArgs g) {
+  constexpr bool IND = K == SR_QSORTI;
+  __shared__ T s_val[SF_WARPS][SF_MAX];
+  __shared__ int32_t s_ix[SF_WARPS][SF_MAX];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  T *const v = s_val[w];
+  int32_t *const ix = s_ix[w];
+  const Bad<T> bv{from_bits<T>(g.abad), (bool)g.abad_isnan};
+  const T obad = from_bits<T>(g.obad);
+  const int n = (int)g.n;
+  const unsigned lt = (1u << lane) - 1u;
+  for (int64_t row = (int64_t)blockIdx.x * SF_WARPS + w; row < g.rows;
+       row += (int64_t)gridDim.x * SF_WARPS) {
+    int64_t offs[MAXP];
+    loop_offsets(g.L, row, offs);
+    const T *a = reinterpret_cast<const T *>(g.a) + offs[0];
+    // good values compacted in order (qsorti: the row as is, good
+    // positions compacted in ix, bad positions straight to the output)
+    int nn = 0, nbad = 0;
+    bool unsafe = false, neg0 = false, pos0 = false;
+    for (int base = 0; base < n; base += 32) {
+      const int t = base + lane;
+      T x = (T)0;
+      bool good = false;
+      if (t < n) {
+        x = a[(int64_t)t * g.inc_a];
+        good = !(K != SR_MODE && BAD && bv.is(x));
+      }
+      const unsigned gm = __ballot_sync(0xffffffffu, good);
+      const unsigned bm = __ballot_sync(0xffffffffu, t < n && !good);
+      if (good) {
+        const int pos = nn + __popc(gm & lt);
+        if constexpr (IND) ix[pos] = t;
+        else v[pos] = x;
+        unsafe |= sf_unsafe_float<T>(x, neg0, pos0);
+      }
+      if constexpr (IND) {
+        if (t < n) v[t] = x;
+        if (t < n && !good)
+          reinterpret_cast<int64_t *>(g.b)[offs[g.out_pdl] +
+                                           (int64_t)(n - 1 - (nbad + __popc(bm & lt))) * g.inc_b] = t;
+      }
+      nn += __popc(gm);
+      nbad += __popc(bm);
+    }
+    unsafe = __any_sync(0xffffffffu, unsafe) ||
+             (__any_sync(0xffffffffu, neg0) && __any_sync(0xffffffffu, pos0));
+    __syncwarp();
+    // bitonic sort of positions [0, P): (key, position) in lexicographic
+    // order, positions >= nn after everything
+    int P = 1;
+    while (P < nn) P <<= 1;
+    if (!unsafe && nn > 1) {
+      if constexpr (!IND) {
+        for (int i = nn + lane; i < P; i += 32) v[i] = (T)0;
+        for (int i = lane; i < P; i += 32) ix[i] = i;  // tie-break by position
+      }
+      for (int i = nn + lane; i < P; i += 32) {
+        if constexpr (IND) ix[i] = -1;
+      }
+      __syncwarp();
+      for (int k = 2; k <= P; k <<= 1) {
+        for (int j = k >> 1; j > 0; j >>= 1) {
+          for (int i = lane; i < P; i += 32) {
+            const int l = i ^ j;
+            if (l > i) {
+              bool greater;  // element i after element l
+              if constexpr (IND) {
+                const int32_t pi = ix[i], pl = ix[l];
+                if (pi < 0) greater = pl >= 0;
+                else if (pl < 0) greater = false;
+                else greater = v[pl] < v[pi] || (v[pl] == v[pi] && pl < pi);
+              } else {
+                const int32_t pi = ix[i], pl = ix[l];
+                const bool si = pi >= nn, sl = pl >= nn;
+                if (si || sl) greater = si && (!sl || pl < pi);
+                else greater = v[l] < v[i] || (v[l] == v[i] && pl < pi);
+              }
+              if (greater == ((i & k) == 0)) {
+                if constexpr (!IND) {
+                  const T tv = v[i];
+                  v[i] = v[l];
+                  v[l] = tv;
+                }
+                const int32_t tp = ix[i];
+                ix[i] = ix[l];
+                ix[l] = tp;
+              }
+            }
+          }
+          __syncwarp();
         }
       }
-      *out = curmode;
-      continue;
-    }
-    if (nn == 0) {
-      *out = obad;  // a row with no good element (bad-value mode only)
-      continue;
-    }
-    const int64_t last = nn - 1;
-    if constexpr (K == SR_MED) {
-      const int64_t n1 = last / 2;
-      *out = last % 2 == 0 ? tmp[n1] : half_sum<T>(tmp[n1], tmp[n1 + 1]);
-    } else if constexpr (K == SR_ODDMED) {
-      *out = tmp[last / 2];
-    } else if constexpr (K == SR_PCT) {
-      const T p = *(reinterpret_cast<const T *>(g.p) + offs[1]);
-      // the reference's mixed-type arithmetic, step by step
-      const double np = last * p;
-      const double lo0 = 0 > np ? 0 : np, lo1 = 0 > np + 1 ? 0 : np + 1;
-      const int64_t n1 = (int64_t)(last < lo0 ? (double)last : lo0);
-      const int64_t n2 = (int64_t)(last < lo1 ? (double)last : lo1);
-      double pp1 = 0, pp2 = 0;
-      if (last != 0) {
-        pp1 = (double)n1 / (double)last;
-        pp2 = (double)n2 / (double)last;
+      if constexpr (IND) {
+        // equal values: the reference's order of their indices is its own
+        bool tie = false;
+        for (int i = lane; i + 1 < nn; i += 32) tie |= v[ix[i]] == v[ix[i + 1]];
+        if (__any_sync(0xffffffffu, tie)) {
+          unsafe = true;
+          // the good positions in order again
+          int m = 0;
+          for (int base = 0; base < n; base += 32) {
+            const int t = base + lane;
+            const bool good = t < n && !(BAD && bv.is(v[t]));
+            const unsigned gm = __ballot_sync(0xffffffffu, good);
+            if (good) ix[m + __popc(gm & lt)] = t;
+            m += __popc(gm);
+          }
+          __syncwarp();
+        }
       }
-      T r;
-      if (np <= 0.0) r = tmp[0];
-      else if (np >= last) r = tmp[last];
-      else if (tmp[n2] == tmp[n1]) r = tmp[n1];
-      else if (p == pp1) r = tmp[n1];
-      else if (p == pp2) r = tmp[n2];
-      else  // no contraction into a fused multiply-add, as in the reference's C
-        r = (T)__dadd_rn(__dmul_rn(np - (double)n1, (double)(tmp[n2] - tmp[n1])),
-                         (double)tmp[n1]);
-      *out = r;
-    } else {  // SR_ODDPCT
-      const T p = *(reinterpret_cast<const T *>(g.p) + offs[1]);
-      const auto q = (last + 1) * p;
-      const auto m = last < q ? (decltype(q))last : q;
-      const int64_t np = (int64_t)(0 > m ? (decltype(q))0 : m);
-      *out = tmp[np];
     }
+    if (unsafe && nn > 1 && lane == 0) {
+      bool ok;
+      if constexpr (IND) ok = qs_indices<T, int32_t>(v, ix, 0, nn - 1);
+      else ok = qs_values<T>(v, 0, nn - 1);
+      if (!ok) atomicOr(g.err, 1);
+    }
+    __syncwarp();
+    if constexpr (IND) {
+      int64_t *out = reinterpret_cast<int64_t *>(g.b) + offs[g.out_pdl];
+      for (int i = lane; i < nn; i += 32) out[(int64_t)i * g.inc_b] = ix[i];
+    } else {
+      T *out = reinterpret_cast<T *>(g.b) + offs[g.out_pdl];
+      finish_values<T, K>(g, v, nn, offs, out, obad, lane, 32);
+    }
+    __syncwarp();
   }
 }
 
@@ -221,6 +383,15 @@ template <class T, int K>
 pdlgb300_error go_sort(const SortArgs &g, cudaStream_t s) {
   pdlgb300_error e = pgh::ok();
   const int nsm = pgh::num_sms();
+  if (g.n <= SF_MAX) {
+    const int64_t grid =
+        std::max<int64_t>(1, std::min<int64_t>((g.rows + SF_WARPS - 1) / SF_WARPS, (int64_t)nsm * 32));
+    if (g.bad) k_sortred_warp<T, K, true><<<(int)grid, SF_WARPS * 32, 0, s>>>(g);
+    else k_sortred_warp<T, K, false><<<(int)grid, SF_WARPS * 32, 0, s>>>(g);
+    if (!pgh::cuda_check(cudaGetLastError(), &e, "k_sortred_warp")) return e;
+    pgh::record_kernel("k_sortred_warp", grid, SF_WARPS * 32);
+    return e;
+  }
   const int64_t grid = std::max<int64_t>(1, std::min<int64_t>((g.rows + 127) / 128, (int64_t)nsm * 16));
   if (g.bad) k_sortred<T, K, true><<<(int)grid, 128, 0, s>>>(g);
   else k_sortred<T, K, false><<<(int)grid, 128, 0, s>>>(g);
