@@ -200,6 +200,17 @@ pdlgb300_error pdlgb300_run_pctover(pdlgb300_ndarray *a, pdlgb300_ndarray *p,
 pdlgb300_error pdlgb300_run_oddpctover(pdlgb300_ndarray *a, pdlgb300_ndarray *p,
                                        pdlgb300_ndarray *b);
 pdlgb300_error pdlgb300_run_modeover(pdlgb300_ndarray *data, pdlgb300_ndarray *out);
+/* lib/PDL/IO/FastRaw.pm:202-323: FastRaw files.  The header ("<name>.hdr"
+ * unless `header` names one) holds "<type id>\n<ndims>\n<dim0> <dim1> ...\n".
+ *   pdlgb300_fraw_header  -- shape and type x from the header (_read_frawhdr)
+ *   pdlgb300_readfraw_into -- the file's bytes into x's memory: host `data`,
+ *     or device `ddata` streamed through pinned staging buffers with the
+ *     disk reads overlapping the copies (readfraw, without a pageable host
+ *     copy); a short file leaves the rest zero, as readfraw's zeroes() does
+ *   pdlgb300_writefraw    -- header and data of a contiguous x (writefraw)  */
+pdlgb300_error pdlgb300_fraw_header(const char *name, const char *header, pdlgb300_ndarray *x);
+pdlgb300_error pdlgb300_readfraw_into(const char *name, pdlgb300_ndarray *x);
+pdlgb300_error pdlgb300_writefraw(const pdlgb300_ndarray *x, const char *name, const char *header);
 /* A deferred expression of PDL::Ops binary ops (lib/PDL/Ops.pd:104-153,
  * 288-307) reduced over dim 0 by a PDL::Ufunc reduction in one pass, with
  * the result the ops and the reduction give one after the other

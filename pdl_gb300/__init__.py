@@ -24,6 +24,10 @@ from .whole import (  # noqa: F401
     all, and_, any, avg, band, bor, bxor, davg, dprod, dsum, max, median, min, mode, oddmedian,
     oddpct, or_, pct, prod, sum, xorall, zcheck)
 from .lazy import Lazy, lazy  # noqa: F401
+from .fastraw import gluefraw, readfraw, writefraw  # noqa: F401
 from ._abi import MATMULT_BF16X3, MATMULT_BF16X6, MATMULT_SIMT_EXACT, MATMULT_SIMT_FP32  # noqa: F401
 
-__all__ = [n for n in dir() if not n.startswith("_")]
+# `from pdl_gb300 import *` leaves Python's builtins alone: the whole-array
+# functions named like builtins stay reachable as pdl_gb300.sum etc.
+_BUILTIN_NAMES = {"sum", "min", "max", "any", "all"}
+__all__ = [n for n in dir() if not n.startswith("_") and n not in _BUILTIN_NAMES]

@@ -102,6 +102,9 @@ SIGNATURES = {
     "pdlgb300_run_pctover": (Error, [P, P, P]),
     "pdlgb300_run_oddpctover": (Error, [P, P, P]),
     "pdlgb300_run_modeover": (Error, [P, P]),
+    "pdlgb300_fraw_header": (Error, [C.c_char_p, C.c_char_p, P]),
+    "pdlgb300_readfraw_into": (Error, [C.c_char_p, P]),
+    "pdlgb300_writefraw": (Error, [P, C.c_char_p, C.c_char_p]),
     "pdlgb300_run_expr_reduce": (Error, [C.POINTER(Vtable), C.c_int32, PP, C.c_int32, C.c_void_p, P]),
     **{f"pdlgb300_run_{op}": (Error, [P, P])
        for op in ("andover", "orover", "xorover", "zcover", "bandover", "borover",

@@ -1,0 +1,84 @@
+"""PDL::IO::FastRaw (lib/PDL/IO/FastRaw.pm:198-350): an ndarray's bytes in
+one file and a text header beside it ("<name>.hdr" unless `header` names
+another file: type id, ndims, dims).  readfraw(device=True) streams the
+file into device memory through pinned staging buffers (the disk reads
+overlap the copies), so the data is never held in a pageable host copy."""
+from __future__ import annotations
+
+import ctypes as C
+import importlib
+import os
+from typing import Optional
+
+import numpy as np
+
+from . import _abi as A
+from ._abi import PDLError, check, lib
+
+N = importlib.import_module(".ndarray", __package__)
+
+
+def _enc(s: Optional[str]):
+    return None if s is None else os.fsencode(s)
+
+
+def read_header(name: str, header: Optional[str] = None):
+    """(type code, dims) from a FastRaw header (_read_frawhdr)."""
+    d = A.Ndarray()
+    check(lib().pdlgb300_fraw_header(_enc(name), _enc(header), C.byref(d)))
+    return d.datatype, tuple(d.dims[i] for i in range(d.ndims))
+
+
+def readfraw(name: str, header: Optional[str] = None, device: bool = False) -> "N.ndarray":
+    """The ndarray in `name` (readfraw); device=True puts it in device memory."""
+    t, dims = read_header(name, header)
+    n = int(np.prod(dims, dtype=np.int64)) if dims else 1
+    if device:
+        x = N.device_empty(t, *dims)
+    else:
+        nbytes = n * np.dtype(N.NP_DTYPES[t]).itemsize
+        x = N.ndarray(N.Storage(nbytes, host=np.zeros(max(nbytes, 1), np.uint8)), t, dims)
+    d = x._desc(device)
+    check(lib().pdlgb300_readfraw_into(_enc(name), C.byref(d)))
+    x.storage.fresh = "dev" if device else "host"
+    return x
+
+
+def _contiguous(x: "N.ndarray") -> "N.ndarray":
+    s = 1
+    for d, i in zip(x.dims, x.incs):
+        if d > 1 and i != s:
+            return N.convert(x, x.datatype)
+        s *= d
+    return x
+
+
+def writefraw(x: "N.ndarray", name: str, header: Optional[str] = None) -> None:
+    """The header and the data of x (writefraw), from host or device memory."""
+    x = _contiguous(x)
+    d = x._desc(x.on_device)
+    check(lib().pdlgb300_writefraw(C.byref(d), _enc(name), _enc(header)))
+
+
+def gluefraw(x: "N.ndarray", name: str, header: Optional[str] = None) -> None:
+    """Append x as one more step of the last dim of the file's ndarray
+    (gluefraw, FastRaw.pm:326-346), with the reference's checks."""
+    if not os.path.isfile(name):
+        raise PDLError(A.EUSERERROR, f"'{name}' must be real filename")
+    t, dims = read_header(name, header)
+    if x.datatype != t:
+        raise PDLError(A.EUSERERROR, f"gluefraw: ndarray has type '{x.type}' but file has type '{t}'")
+    if len(dims) < 2:
+        raise PDLError(A.EUSERERROR, f"gluefraw: header dims needs at least 2 dims, got ({' '.join(map(str, dims))})")
+    low = dims[:-1]
+    shape = tuple(x.dims) + (1,) * max(0, len(low) - x.ndims)
+    if len(x.dims) > len(low) or tuple(shape[: len(low)]) != tuple(low):
+        raise PDLError(A.EUSERERROR,
+                       f"gluefraw: incompatible lower dims, ndarray ({' '.join(map(str, x.dims))}) "
+                       f"vs header ({' '.join(map(str, low))})")
+    with open(name, "ab") as f:
+        f.write(np.ascontiguousarray(x.numpy()).tobytes())
+    new_dims = list(dims[:-1]) + [dims[-1] + 1]
+    hname = header or name + ".hdr"
+    with open(hname, "w") as h:
+        h.write(f"{t}\n{len(new_dims)}\n{' '.join(map(str, new_dims))}\n")

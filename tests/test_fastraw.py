@@ -1,0 +1,77 @@
+"""PDL::IO::FastRaw through the C ABI on host memory (no GPU): the cases of
+the reference's t/fastraw.t (write then read back, gluefraw, a custom
+header), the header text exactly as _writefrawhdr writes it, a short file
+read as zeroes, and the header errors.  Device-resident reads and writes,
+and views (written through a device copy), are in test_gpu_fastraw.py."""
+import numpy as np
+import pytest
+
+import pdl_gb300 as P
+
+
+def startdata():
+    return P.pdl(np.array([[2.0, 3], [4, 5], [6, 7]]))    # PDL dims (2, 3)
+
+
+def test_write_read_round_trip(tmp_path):
+    name = str(tmp_path / "tmp0")
+    x = startdata()
+    P.writefraw(x, name)
+    assert (tmp_path / "tmp0").is_file() and (tmp_path / "tmp0.hdr").is_file()
+    # type id (double = 10 in PDL's order), ndims, dims
+    assert (tmp_path / "tmp0.hdr").read_text() == "10\n2\n2 3\n"
+    y = P.readfraw(name)
+    assert y.type == "double" and y.dims == (2, 3)
+    assert np.array_equal(y.numpy(), x.numpy())
+
+
+def test_gluefraw(tmp_path):
+    name = str(tmp_path / "tmp0.g")
+    P.writefraw(startdata(), name)
+    P.gluefraw(P.pdl(np.array([10.0, 11])), name)
+    y = P.readfraw(name)
+    assert np.array_equal(y.numpy(), np.array([[2.0, 3], [4, 5], [6, 7], [10, 11]]))
+    with pytest.raises(P.PDLError, match="has type 'long' but file has type"):
+        P.gluefraw(P.pdl(np.array([1, 2], np.int32)), name)
+    with pytest.raises(P.PDLError, match="incompatible lower dims"):
+        P.gluefraw(P.pdl(np.array([1.0, 2, 3])), name)
+
+
+def test_custom_header(tmp_path):
+    name, header = str(tmp_path / "tmp0"), str(tmp_path / "headerfile")
+    x = startdata()
+    P.writefraw(x, name, header=header)
+    assert (tmp_path / "headerfile").is_file() and not (tmp_path / "tmp0.hdr").exists()
+    assert np.array_equal(P.readfraw(name, header=header).numpy(), x.numpy())
+
+
+NP = {"byte": np.uint8, "short": np.int16, "long": np.int32, "longlong": np.int64,
+      "float": np.float32, "double": np.float64}
+
+
+@pytest.mark.parametrize("t", list(NP))
+def test_types(tmp_path, t):
+    a = np.random.default_rng(0).integers(0, 100, size=(4, 5, 6)).astype(NP[t])
+    x = P.pdl(a)
+    name = str(tmp_path / f"f_{t}")
+    P.writefraw(x, name)
+    y = P.readfraw(name)
+    assert y.type == t and y.dims == (6, 5, 4)
+    assert np.array_equal(y.numpy(), a)
+
+
+def test_short_file_reads_zeroes_and_header_errors(tmp_path):
+    name = str(tmp_path / "short")
+    (tmp_path / "short").write_bytes(np.array([1.5, 2.5], np.float64).tobytes())
+    (tmp_path / "short.hdr").write_text("10\n1\n4\n")
+    assert P.readfraw(name).numpy().tolist() == [1.5, 2.5, 0.0, 0.0]
+    (tmp_path / "bad.hdr").write_text("10\n2\n4\n")
+    (tmp_path / "bad").write_bytes(b"")
+    with pytest.raises(P.PDLError, match="Format error reading fraw header file"):
+        P.readfraw(str(tmp_path / "bad"))
+    (tmp_path / "trunc.hdr").write_text("10\n1\n")
+    (tmp_path / "trunc").write_bytes(b"")
+    with pytest.raises(P.PDLError, match="Format error in"):
+        P.readfraw(str(tmp_path / "trunc"))
+    with pytest.raises(P.PDLError, match="Couldn't open"):
+        P.readfraw(str(tmp_path / "missing"))

@@ -1,0 +1,51 @@
+"""FastRaw straight to and from device memory: the file streamed through
+the pinned staging buffers into a device-resident ndarray (and a file of
+several staging chunks), device-resident data written out, and a view
+written through a contiguous device copy."""
+import numpy as np
+import pytest
+
+import pdl_gb300 as P
+
+pytestmark = pytest.mark.gpu
+
+
+def test_device_round_trip(gpu, tmp_path):
+    a = np.random.default_rng(1).standard_normal((300, 257)).astype(np.float32)
+    x = P.pdl(a).to_device()
+    name = str(tmp_path / "dev")
+    P.writefraw(x, name)
+    assert (tmp_path / "dev.hdr").read_text() == "9\n2\n257 300\n"
+    y = P.readfraw(name, device=True)
+    assert y.on_device and y.type == "float" and y.dims == (257, 300)
+    assert np.array_equal(y.numpy(), a)
+    # a reduction runs on the device-resident result directly
+    assert np.allclose(P.sumover(y).numpy(), a.astype(np.float64).sum(-1), rtol=1e-5, atol=1e-4)
+
+
+def test_device_read_of_several_chunks(gpu, tmp_path):
+    # 80 MiB: three 32 MiB staging chunks, the last one partial
+    n = 80 * (1 << 20) // 8
+    a = np.arange(n, dtype=np.int64)
+    name = str(tmp_path / "big")
+    a.tofile(name)
+    (tmp_path / "big.hdr").write_text(f"8\n1\n{n}\n")
+    y = P.readfraw(name, device=True)
+    got = y.numpy()
+    assert got.dtype == np.int64 and np.array_equal(got, a)
+
+
+def test_device_short_file_is_zero_filled(gpu, tmp_path):
+    name = str(tmp_path / "short")
+    np.array([1.5, 2.5], np.float64).tofile(name)
+    (tmp_path / "short.hdr").write_text("10\n1\n5\n")
+    assert P.readfraw(name, device=True).numpy().tolist() == [1.5, 2.5, 0.0, 0.0, 0.0]
+
+
+def test_view_written_contiguously(gpu, tmp_path):
+    a = np.arange(120, dtype=np.int32).reshape(4, 5, 6)
+    v = P.pdl(a).xchg(0, 2)
+    name = str(tmp_path / "view")
+    P.writefraw(v, name)
+    y = P.readfraw(name)
+    assert y.dims == v.dims and np.array_equal(y.numpy(), v.numpy())
