@@ -130,9 +130,9 @@ class Clocks:
             except Exception:
                 self.proc.kill()
             self.th.join(timeout=2)
-        out = ROOT / "gpurun_out"
-        if out.exists():
-            with open(out / "bench_clocks.csv", "a") as f:
+        log = os.environ.get("PDLGB300_CLOCKS_LOG")
+        if log:  # the raw samples, appended for the record
+            with open(log, "a") as f:
                 f.write("\n".join(self.lines) + "\n")
 
     def summary(self):
