@@ -128,3 +128,29 @@ def test_oracle_threads_agree():
         r1 = O.run(op, [a], nthreads=1)[0].numpy()
         r8 = O.run(op, [a], nthreads=8)[0].numpy()
         assert np.array_equal(r1, r8, equal_nan=True), op
+
+
+def test_oracle_sort_functions_against_numpy():
+    """Properties any correct sort satisfies, on data without NaN or mixed
+    zeros: qsort is numpy's sorted row, qsorti a permutation that sorts
+    the row, medover the middle value (the mean of the two middle ones
+    for an even count, in the type's arithmetic), oddmedover the lower
+    middle, modeover the most frequent repeated value."""
+    rng = np.random.default_rng(11)
+    for n in (1, 2, 7, 64, 301):
+        a = rng.integers(-20, 20, size=(9, n)).astype(np.float64)
+        x = P.pdl(a)
+        s = np.sort(a, -1)
+        assert np.array_equal(O.run("qsort", [x])[0].numpy(), s)
+        ix = O.run("qsorti", [x])[0].numpy()
+        assert np.array_equal(np.take_along_axis(a, ix, -1), s)
+        assert all(sorted(r) == list(range(n)) for r in ix.tolist())
+        lo, hi = s[:, (n - 1) // 2], s[:, n // 2]
+        assert np.array_equal(O.run("medover", [x])[0].numpy(), 0.5 * (lo + hi))
+        assert np.array_equal(O.run("oddmedover", [x])[0].numpy(), lo)
+        xi = P.pdl(a.astype(np.int32))
+        mo = O.run("modeover", [xi])[0].numpy()
+        for r, m in zip(a.astype(np.int32), mo):
+            vals, cnt = np.unique(r, return_counts=True)
+            want = vals[np.argmax(cnt)] if cnt.max() > 1 else 0
+            assert m == want
