@@ -298,6 +298,10 @@ class LazyLeaf:
     def __init__(self, x: N.ndarray):
         self.x = x
 
+    def __getattr__(self, name):
+        # anything but a binary op (a reduction, dims, numpy()) is the ndarray's
+        return getattr(self.x, name)
+
     def __add__(self, o): return Lazy("plus", self.x, _unwrap(o))
     def __radd__(self, o): return Lazy("plus", _unwrap(o), self.x)
     def __mul__(self, o): return Lazy("mult", self.x, _unwrap(o))

@@ -42,3 +42,11 @@ def test_not_fused_programs():
     assert e._program() is None                               # five leaves
     f = P.lazy(P.pdl(np.zeros(4, np.float32))) + P.pdl(np.zeros(4))
     assert f.type == "double" and f._program() is None        # a float leaf converted
+
+
+def test_leaf_forwards_everything_but_ops():
+    a = P.pdl(np.arange(6.0).reshape(2, 3))
+    leaf = P.lazy(a)
+    assert leaf.dims == (3, 2) and leaf.type == "double"
+    assert np.array_equal(leaf.numpy(), a.numpy())
+    assert isinstance(leaf + 1, P.Lazy)
