@@ -116,7 +116,7 @@ enum {
   OP_ANDOVER, OP_OROVER, OP_XOROVER, OP_ZCOVER, OP_BANDOVER, OP_BOROVER,
   OP_BXOROVER, OP_FIRSTNONZEROOVER, OP_CUMUPRODOVER, OP_DCUMUPRODOVER,
   OP_MINMAXIMUM, OP_QSORT, OP_QSORTI, OP_MEDOVER, OP_ODDMEDOVER, OP_PCTOVER,
-  OP_ODDPCTOVER, OP_MODEOVER,
+  OP_ODDPCTOVER, OP_MODEOVER, OP_QSORTVEC, OP_QSORTVECI,
   OP_N
 };
 #define IS_BIOP(op) ((op) == OP_PLUS || (op) == OP_MULT || ((op) >= OP_MINUS && (op) <= OP_XOR))
@@ -191,6 +191,9 @@ static const opdef OPS[OP_N] = {
   {"pctover", 3, 2, {"a", "p", "b"}, {1, 0, 0}, {{0}, {0}, {0}}, {"n"}, 0, -1},
   {"oddpctover", 3, 2, {"a", "p", "b"}, {1, 0, 0}, {{0}, {0}, {0}}, {"n"}, 0, -1},
   {"modeover", 2, 1, {"data", "out"}, {1, 0}, {{0}, {0}}, {"n"}, 0, -1, 1},
+  /* lib/PDL/Ufunc.pd:1115-1230: a list of m vectors of n, sorted lexicographically */
+  {"qsortvec", 2, 1, {"a", "b"}, {2, 2}, {{0, 1}, {0, 1}}, {"n", "m"}, 0, -1},
+  {"qsortveci", 2, 1, {"a", "indx"}, {2, 1}, {{0, 1}, {1}}, {"n", "m"}, TYPED, PDLGB300_IND},
 };
 
 static int find_op(const char *name) {
@@ -1110,6 +1113,110 @@ O_INT_TYPES(DEF_MODEOVERS)
 #define modeover_F NULL
 #define modeover_D NULL
 
+/* ------------------------------------------ vector sorts (Ufunc.pd:769-851)
+ * PDL_QSORTVEC: the pivot is the vector at position median_ind, compared
+ * in place (not copied), and median_ind follows that vector when a swap
+ * moves it; vectors compare lexicographically (pdl_cmpvec).  The two
+ * ranges after a partition are disjoint, so their order does not matter. */
+#define DEF_QSORTVEC(T, SYM, ISF)                                                    \
+  static int ocmpvec_##SYM(const T *a, const T *b, int64_t n) {                     \
+    for (int64_t i = 0; i < n; i++) {                                                \
+      if (a[i] < b[i]) return -1;                                                    \
+      if (a[i] > b[i]) return 1;                                                     \
+    }                                                                                \
+    return 0;                                                                        \
+  }                                                                                  \
+  static void oqv_##SYM(T *xx, int64_t n, int64_t a, int64_t b) {                   \
+    int64_t i = a, j = b, med = (i + j) / 2;                                         \
+    do {                                                                             \
+      while (ocmpvec_##SYM(xx + n * i, xx + n * med, n) < 0) i++;                    \
+      while (ocmpvec_##SYM(xx + n * j, xx + n * med, n) > 0) j--;                    \
+      if (i <= j) {                                                                  \
+        for (int64_t k = 0; k < n; k++) {                                            \
+          T z = xx[n * i + k]; xx[n * i + k] = xx[n * j + k]; xx[n * j + k] = z;     \
+        }                                                                            \
+        if (med == i) med = j;                                                       \
+        else if (med == j) med = i;                                                  \
+        i++; j--;                                                                    \
+      }                                                                              \
+    } while (i <= j);                                                                \
+    if (a < j) oqv_##SYM(xx, n, a, j);                                               \
+    if (i < b) oqv_##SYM(xx, n, i, b);                                               \
+  }                                                                                  \
+  static void oqvi_##SYM(const T *xx, int64_t *ix, int64_t n, int64_t a, int64_t b) { \
+    int64_t i = a, j = b, med = (i + j) / 2;                                         \
+    do {                                                                             \
+      while (ocmpvec_##SYM(xx + n * ix[i], xx + n * ix[med], n) < 0) i++;            \
+      while (ocmpvec_##SYM(xx + n * ix[j], xx + n * ix[med], n) > 0) j--;            \
+      if (i <= j) {                                                                  \
+        int64_t z = ix[i]; ix[i] = ix[j]; ix[j] = z;                                 \
+        if (med == i) med = j;                                                       \
+        else if (med == j) med = i;                                                  \
+        i++; j--;                                                                    \
+      }                                                                              \
+    } while (i <= j);                                                                \
+    if (a < j) oqvi_##SYM(xx, ix, n, a, j);                                          \
+    if (i < b) oqvi_##SYM(xx, ix, n, i, b);                                          \
+  }                                                                                  \
+  /* qsortvec: good vectors in order, vectors with a bad element from the end */  \
+  static void qsortvec_##SYM(octx *c, const int64_t *offs, int64_t n0, const int64_t *inc0) { \
+    int64_t N = c->ind_sizes[0], M = c->ind_sizes[1];                                \
+    int64_t ian = c->inc_sizes[0][0], iam = c->inc_sizes[0][1];                      \
+    int64_t ibn = c->inc_sizes[1][0], ibm = c->inc_sizes[1][1];                      \
+    T abad = c->bad[0].SYM, bbad = c->bad[1].SYM;                                    \
+    T *tmp = (T *)malloc(sizeof(T) * (N * M > 0 ? N * M : 1));                           \
+    for (int64_t i0 = 0; i0 < n0; i0++) {                                            \
+      const T *a = (const T *)c->base[0] + offs[0] + i0 * inc0[0];                   \
+      T *b = (T *)c->base[1] + offs[1] + i0 * inc0[1];                               \
+      if (N * M == 0) continue;                                                      \
+      int64_t nn = 0, nb = M - 1;                                                    \
+      for (int64_t m = 0; m < M; m++) {                                              \
+        int good = 1;                                                                \
+        if (c->bvalflag)                                                             \
+          for (int64_t k = 0; k < N; k++)                                            \
+            if (ISBADV(a[k * ian + m * iam], abad, ISF)) { good = 0; break; }        \
+        int64_t d = good ? nn++ : nb--;                                              \
+        for (int64_t k = 0; k < N; k++) {                                            \
+          T v = a[k * ian + m * iam];                                                \
+          tmp[d * N + k] = (c->bvalflag && ISBADV(v, abad, ISF)) ? bbad : v;         \
+        }                                                                            \
+      }                                                                              \
+      if (nn > 0) oqv_##SYM(tmp, N, 0, nn - 1);                                      \
+      for (int64_t m = 0; m < M; m++)                                                \
+        for (int64_t k = 0; k < N; k++) b[k * ibn + m * ibm] = tmp[m * N + k];       \
+    }                                                                                \
+    free(tmp);                                                                       \
+  }                                                                                  \
+  static void qsortveci_##SYM(octx *c, const int64_t *offs, int64_t n0, const int64_t *inc0) { \
+    int64_t N = c->ind_sizes[0], M = c->ind_sizes[1];                                \
+    int64_t ian = c->inc_sizes[0][0], iam = c->inc_sizes[0][1];                      \
+    int64_t ibm = c->inc_sizes[1][0];                                                \
+    T abad = c->bad[0].SYM;                                                          \
+    T *tmp = (T *)malloc(sizeof(T) * (N * M > 0 ? N * M : 1));                           \
+    int64_t *ix = (int64_t *)malloc(sizeof(int64_t) * (M ? M : 1));                 \
+    for (int64_t i0 = 0; i0 < n0; i0++) {                                            \
+      const T *a = (const T *)c->base[0] + offs[0] + i0 * inc0[0];                   \
+      int64_t *b = (int64_t *)c->base[1] + offs[1] + i0 * inc0[1];                   \
+      if (N * M == 0) continue;                                                      \
+      int64_t nn = 0, nb = M - 1;                                                    \
+      for (int64_t m = 0; m < M; m++) {                                              \
+        int good = 1;                                                                \
+        for (int64_t k = 0; k < N; k++) {                                            \
+          T v = a[k * ian + m * iam];                                                \
+          tmp[m * N + k] = v;                                                        \
+          if (c->bvalflag && ISBADV(v, abad, ISF)) good = 0;                         \
+        }                                                                            \
+        ix[good ? nn++ : nb--] = m;                                                  \
+      }                                                                              \
+      if (nn > 0) oqvi_##SYM(tmp, ix, N, 0, nn - 1);                                 \
+      for (int64_t m = 0; m < M; m++) b[m * ibm] = ix[m];                            \
+    }                                                                                \
+    free(tmp);                                                                       \
+    free(ix);                                                                        \
+  }
+#define DEF_QSORTVECS(E, CT, SYM, IP, ISF, UNS) DEF_QSORTVEC(CT, SYM, ISF)
+O_REAL_TYPES(DEF_QSORTVECS)
+
 static body_fn pick_body(int op, int t) {
 #define CASE(OPID, PFX)                                                   \
   case OPID:                                                               \
@@ -1170,6 +1277,8 @@ static body_fn pick_body(int op, int t) {
     CASE(OP_PCTOVER, pctover)
     CASE(OP_ODDPCTOVER, oddpctover)
     CASE(OP_MODEOVER, modeover)
+    CASE(OP_QSORTVEC, qsortvec)
+    CASE(OP_QSORTVECI, qsortveci)
   }
 #undef CASE
   return NULL;
