@@ -105,6 +105,23 @@ SHAPE_CASES = [
     ("matmult", [Z("float", 1024, 2048, 16), Z("float", 2048, 1024)]),
     ("matmult", [Z("double", 3, 2, 1, 4), Z("double", 5, 3, 7, 1)]),
     ("sumover_mult_plus", [Z("long", 256, 1, 8192), Z("long", 256, 512, 1), Z("long", 256, 1, 8192)]),
+    # the widened rows: type rules (GenericTypes, typed outputs) and shapes
+    ("minus", [Z("short", 3, 1), Z("float", 1, 4)]),
+    ("gt", [Z("long", 5), Z("double", 5)]),
+    ("shiftleft", [Z("double", 4), Z("byte", 4)]),       # integer types only: longlong
+    ("xor", [Z("float", 2, 3), Z("long", 2, 1)]),
+    ("andover", [Z("float", 6, 2)]),
+    ("bandover", [Z("double", 6, 2)]),                  # integer types only: longlong
+    ("firstnonzeroover", [Z("ushort", 3, 3)]),
+    ("cumuprodover", [Z("byte", 5, 2)]),
+    ("dcumuprodover", [Z("short", 5, 2)]),
+    ("qsort", [Z("float", 7, 3)]),
+    ("qsorti", [Z("byte", 7, 3)]),
+    ("medover", [Z("long", 9, 4, 2)]),
+    ("oddmedover", [Z("double", 9)]),
+    ("pctover", [Z("float", 9, 4), Z("double")]),
+    ("oddpctover", [Z("long", 9, 4), Z("long", 4)]),
+    ("modeover", [Z("double", 7, 2)]),                  # integer types only: longlong
 ]
 
 
@@ -112,7 +129,6 @@ SHAPE_CASES = [
 def test_null_output_shape_and_type_match_oracle(op, inputs):
     got = lib_redodims(op, inputs)
     if op == "sumover_mult_plus":  # composition of mult, plus, sumover
-        t = O.run("mult", inputs[:2])[0] if False else None
         assert got[0] == tuple(max(a, b, c) for a, b, c in
                                zip(*[x.dims[1:] + (1,) * (3 - x.ndims) for x in inputs]))
         return
@@ -130,6 +146,8 @@ ERROR_CASES = [
     ("plus", [Z("double", 2, 2), Z("double", 2)], "dummy", r"implicit dim 1 size 2, but dim is dummy"),
     ("cumusumover", [Z("double", 2, 2)], "dummy0", r"index 'n' size 2, can't broadcast over dummy dim with size > 1"),
     ("matmult", [Z("double", 3, 2), Z("double", 2, 4)], None, r"index 't' size 3, but ndarray dim has size 4"),
+    ("pctover", [Z("double", 5, 3), Z("double", 4)], None, r"Mismatched implicit broadcast dimension 0: size 3 vs\. 4"),
+    ("qsort", [Z("double", 3, 2)], Z("double", 2, 2), r"index 'n' size 3, but ndarray dim has size 2"),
 ]
 
 
