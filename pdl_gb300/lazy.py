@@ -62,6 +62,7 @@ class Lazy:
     def __init__(self, op: str, a, b):
         if op not in BIOPS:
             raise A.PDLError(A.EUSERERROR, f"{op} is not a binary op of PDL::Ops")
+        a, b = _unwrap(a), _unwrap(b)
         like = a if isinstance(a, (Lazy, N.ndarray)) else b if isinstance(b, (Lazy, N.ndarray)) else None
         a = a if isinstance(a, (Lazy, N.ndarray)) else N._scalar_to_pdl(a, _like(like))
         b = b if isinstance(b, (Lazy, N.ndarray)) else N._scalar_to_pdl(b, _like(like))

@@ -50,3 +50,37 @@ def test_leaf_forwards_everything_but_ops():
     assert leaf.dims == (3, 2) and leaf.type == "double"
     assert np.array_equal(leaf.numpy(), a.numpy())
     assert isinstance(leaf + 1, P.Lazy)
+    # a leaf on the right of a recorded op is its ndarray
+    e = (P.lazy(a) * a) + P.lazy(a)
+    assert e.b is a and e._program()[1] == [("mult", 0, 0), ("plus", 1, 0)]
+
+
+def test_random_expressions_shape_and_type_like_the_eager_chain():
+    """Random trees of binary ops over broadcastable leaves of mixed types:
+    each recorded node has the dims and type the oracle's planner gives the
+    eager op on its operands' shapes and types."""
+    from oracle import oracle as O
+    rng = np.random.default_rng(21)
+    types = ["byte", "short", "long", "longlong", "float", "double"]
+    ops = ["plus", "mult", "minus", "divide", "gt", "le", "eq"]
+    bit = ["shiftleft", "or2", "and2", "xor"]
+
+    def leaf():
+        dims = [int(rng.choice([1, 3]))] + ([int(rng.choice([1, 4]))] if rng.random() < 0.6 else [])
+        return P.zeroes(str(rng.choice(types)), *dims)
+
+    def check(e):
+        if not isinstance(e, P.Lazy):
+            return e
+        a, b = check(e.a), check(e.b)
+        dims, t = O.redodims(e.op, [a, b])
+        assert (e.dims, e.datatype) == (tuple(dims), t), (e, dims, t)
+        return P.zeroes(t, *dims)
+
+    for _ in range(200):
+        e = P.lazy(leaf())
+        for _ in range(int(rng.integers(1, 4))):
+            op = str(rng.choice(ops + bit))
+            other = leaf()
+            e = P.Lazy(op, e, other) if rng.random() < 0.5 else P.Lazy(op, other, e)
+        check(e)
