@@ -51,3 +51,37 @@ def test_clump_list_errors():
         x.clump(1, 1)
     with pytest.raises(P.PDLError, match="larger than greatest"):
         x.clump(0, 5)
+
+
+def test_clump_views_against_numpy_on_random_views():
+    """Random slices, exchanges and dummies: every clump that stays a view
+    holds the elements of the view in PDL order (dim 0 fastest); the ones
+    that need a copy are left to the GPU tests."""
+    rng = np.random.default_rng(3)
+    done = 0
+    for _ in range(300):
+        shape = tuple(int(v) for v in rng.integers(1, 5, size=int(rng.integers(1, 4))))
+        a = np.arange(int(np.prod(shape)), dtype=np.float64).reshape(shape)
+        x = P.pdl(a)
+        if rng.random() < 0.4 and x.ndims > 1:
+            i, j = (int(v) for v in rng.choice(x.ndims, 2, replace=False))
+            x = x.xchg(i, j)
+        if rng.random() < 0.3:
+            x = x.dummy(int(rng.integers(0, x.ndims + 1)), int(rng.integers(1, 3)))
+        if rng.random() < 0.3:
+            k = int(rng.integers(0, x.ndims))
+            specs = [slice(None)] * x.ndims
+            specs[k] = slice(None, None, 2)
+            x = x.slice(*specs)
+        n = int(rng.integers(-x.ndims - 1, x.ndims + 2))
+        try:
+            c = x.clump(n)
+        except P.PDLError:
+            continue  # a copy: needs the device
+        v = x.numpy()                              # numpy order: last PDL dim first
+        nd = x.ndims
+        m = nd if n == -1 else (max(nd + n + 1, 0) if n < -1 else min(n, nd))
+        want = v.reshape(v.shape[: nd - m] + (-1,)) if m else v[..., None]
+        assert c.numpy().shape == want.shape and np.array_equal(c.numpy(), want)
+        done += 1
+    assert done > 150
