@@ -84,3 +84,42 @@ def test_random_expressions_shape_and_type_like_the_eager_chain():
             other = leaf()
             e = P.Lazy(op, e, other) if rng.random() < 0.5 else P.Lazy(op, other, e)
         check(e)
+
+
+def _expr_call(red, leaves, nodes, out=None):
+    import ctypes as C
+    from pdl_gb300 import _abi as A
+    from pdl_gb300.lazy import _ExprNode
+    L = A.lib()
+    descs = [x._desc(False) for x in leaves]
+    larr = (A.P * len(descs))(*[C.pointer(d) for d in descs])
+    narr = (_ExprNode * len(nodes))()
+    for k, (op, ia, ib) in enumerate(nodes):
+        narr[k].op = L.pdlgb300_get_vtable(op.encode())
+        narr[k].a, narr[k].b = ia, ib
+    od = A.Ndarray()
+    L.pdlgb300_ndarray_null(C.byref(od))
+    e = L.pdlgb300_run_expr_reduce(L.pdlgb300_get_vtable(red.encode()), len(leaves), larr,
+                                   len(nodes), narr, C.byref(od))
+    return e.error, (e.message.decode() if e.message else "")
+
+
+def test_expression_entry_point_validates_programs():
+    """pdlgb300_run_expr_reduce refuses malformed programs before any
+    device work (host-only checks, no GPU needed)."""
+    a = P.pdl(np.zeros((2, 3)))
+    b = P.pdl(np.zeros((2, 3), np.float32))
+    code, msg = _expr_call("sumover", [a, b], [("plus", 0, 1)])
+    assert code and "leaves of types double and float" in msg
+    code, msg = _expr_call("sumover", [a], [("plus", 0, 1)])
+    assert code and "refers to 1" in msg                     # operand beyond the leaves
+    code, msg = _expr_call("sumover", [a, a], [("plus", 0, 0)])
+    assert code and "leaf 1 does not reach the result" in msg
+    code, msg = _expr_call("sumover", [a], [("sumover", 0, 0)])
+    assert code and "not a binary op" in msg
+    code, msg = _expr_call("cumusumover", [a], [("plus", 0, 0)])
+    assert code and "not a reduction over dim 0" in msg     # a scan: the eager path
+    code, msg = _expr_call("sumover", [a], [("shiftleft", 0, 0)])
+    assert code and "integer type" in msg
+    code, msg = _expr_call("bandover", [a], [("plus", 0, 0)])
+    assert code and "not fused" in msg
