@@ -75,3 +75,26 @@ def test_short_file_reads_zeroes_and_header_errors(tmp_path):
         P.readfraw(str(tmp_path / "trunc"))
     with pytest.raises(P.PDLError, match="Couldn't open"):
         P.readfraw(str(tmp_path / "missing"))
+
+
+def test_zero_dims_header_and_glue_errors(tmp_path):
+    # a 0-dim ndarray: "10\n0\n\n" (_writefrawhdr joins no dims)
+    name = str(tmp_path / "scalar")
+    P.writefraw(P.pdl(np.array(2.5)), name)
+    assert (tmp_path / "scalar.hdr").read_text() == "10\n0\n\n"
+    y = P.readfraw(name)
+    assert y.dims == () and float(y.numpy()) == 2.5
+    # gluefraw wants a file of at least 2 dims (FastRaw.pm:336)
+    one = str(tmp_path / "one")
+    P.writefraw(P.pdl(np.array([1.0, 2.0])), one)
+    with pytest.raises(P.PDLError, match="needs at least 2 dims"):
+        P.gluefraw(P.pdl(np.array([3.0, 4.0])), one)
+    with pytest.raises(P.PDLError, match="must be real filename"):
+        P.gluefraw(P.pdl(np.array([3.0])), str(tmp_path / "nofile"))
+
+
+def test_header_type_outside_this_path(tmp_path):
+    (tmp_path / "ld").write_bytes(b"")
+    (tmp_path / "ld.hdr").write_text("11\n1\n2\n")        # long double
+    with pytest.raises(P.PDLError, match="not on this path"):
+        P.readfraw(str(tmp_path / "ld"))
