@@ -520,7 +520,10 @@ def bench_c2(args, P, torch, stream):
     bad = np.float32(-3.4028234663852886e38)
     af[rng3.random(af.shape) < 0.02] = bad
     bf[rng3.random(bf.shape) < 0.02] = bad
-    for name, (ha, hb, badflag) in {"int32": (a, b, False), "float32_bad": (af, bf, True)}.items():
+    variants = {"int32": (a, b, False), "float32_bad": (af, bf, True)}
+    for name, (ha, hb, badflag) in variants.items():
+        if name not in args.c2_types.split(","):
+            continue
         x, y = P.pdl(ha), P.pdl(hb)
         if badflag:
             x.badflag(1)
@@ -710,6 +713,12 @@ def main():
                     help="time only the deferred-expression workload and print its object")
     ap.add_argument("--sort-only", action="store_true",
                     help="time only the sort-based workload and print its object")
+    ap.add_argument("--family-only", action="store_true",
+                    help="time only the float64 family (--ops) and print its object")
+    ap.add_argument("--c2-only", action="store_true",
+                    help="time only the fused sumover(a*b+a) workload and print its object")
+    ap.add_argument("--c2-types", default="int32,float32_bad",
+                    help="comma-separated subset of int32,float32_bad (for profiling)")
     args = ap.parse_args()
     UFUNC_OPS = [o for o in args.ops.split(",") if o]
     rank = int(os.environ.get("RANK", 0))
@@ -719,12 +728,15 @@ def main():
             return 0
         print(json.dumps(run_reference(args, rank, world)))
         return 0
-    if args.expr_only or args.sort_only:
+    if args.expr_only or args.sort_only or args.family_only or args.c2_only:
         import torch
         import pdl_gb300 as P
         stream = torch.cuda.current_stream()
         P.set_stream(stream.cuda_stream)
-        fn = bench_expr if args.expr_only else bench_sort
+        if args.c2_only:
+            print(json.dumps(bench_c2(args, P, torch, stream)))
+            return 0
+        fn = bench_expr if args.expr_only else bench_sort if args.sort_only else run_family
         print(json.dumps(fn(args, P, torch, stream, peaks()[0])))
         return 0
     if world > 1:

@@ -207,7 +207,10 @@ pdlgb300_error pdlgb300_run_modeover(pdlgb300_ndarray *data, pdlgb300_ndarray *o
  *     or device `ddata` streamed through pinned staging buffers with the
  *     disk reads overlapping the copies (readfraw, without a pageable host
  *     copy); a short file leaves the rest zero, as readfraw's zeroes() does
- *   pdlgb300_writefraw    -- header and data of a contiguous x (writefraw)  */
+ *   pdlgb300_writefraw    -- header and data of a contiguous x (writefraw)
+ * Device-memory transfers of one device share its two pinned staging
+ * buffers: concurrent calls from several host threads are safe but take
+ * turns (each holds the buffers for its whole transfer).  */
 pdlgb300_error pdlgb300_fraw_header(const char *name, const char *header, pdlgb300_ndarray *x);
 pdlgb300_error pdlgb300_readfraw_into(const char *name, pdlgb300_ndarray *x);
 pdlgb300_error pdlgb300_writefraw(const pdlgb300_ndarray *x, const char *name, const char *header);
@@ -314,8 +317,11 @@ pdlgb300_error pdlgb300_matmult_bwd(const pdlgb300_ndarray *gc, const pdlgb300_n
  * held until the process exits); it calls no allocator.
  * - a and b must be device-resident (ddata set); b must already have
  *   sumover's output shape and type (no null output, no conversion).
- * - Rows are limited by the scratch: a call needing more than 1 MiB of
- *   partials (two per row at least) returns PDLGB300_EUSERERROR.
+ * - Rows are limited by the scratch: at most (1048576 - 256) / (2 * unit)
+ *   rows, unit = accumulator + 8-byte count (16 bytes for float64,
+ *   compensated float32 and 64-bit integers: 32760 rows; 12 bytes
+ *   otherwise: 43680 rows).  More returns PDLGB300_EUSERERROR, whose text
+ *   states the limit for the type.
  * - The first call on a device looks the array's device address up
  *   (cudaGetSymbolAddress); make that first call before any stream capture.
  * - Every call shares the array (it keeps the last call's partials; each

@@ -42,10 +42,13 @@ bool read_line(FILE *f, std::string &out) {
   return any;
 }
 
-// two pinned buffers and their events, per device, made on first use
+// two pinned buffers and their events, per device, made on first use; a
+// staged transfer holds `use` from its first refill to its last copy, so
+// host threads reading or writing files on one device take turns
 struct Staging {
   void *buf[2] = {nullptr, nullptr};
   cudaEvent_t ev[2] = {nullptr, nullptr};
+  std::mutex use;
 };
 std::mutex g_stage_mu;
 Staging g_stage[64];
@@ -153,6 +156,11 @@ pdlgb300_error pdlgb300_readfraw_into(const char *name, pdlgb300_ndarray *x) {
   }
   Staging *s = nullptr;
   e = staging(&s);
+  if (e.error) {
+    fclose(f);
+    return e;
+  }
+  std::lock_guard<std::mutex> turn(s->use);
   char *dst = (char *)x->ddata;
   int k = 0;
   while (!e.error && got < len) {
@@ -217,6 +225,11 @@ pdlgb300_error pdlgb300_writefraw(const pdlgb300_ndarray *x, const char *name, c
   }
   Staging *st = nullptr;
   e = staging(&st);
+  if (e.error) {
+    fclose(f);
+    return e;
+  }
+  std::lock_guard<std::mutex> turn(st->use);
   const char *src = (const char *)x->ddata + x->offs * (int64_t)ts;
   size_t done = 0;
   while (!e.error && done < len) {

@@ -60,6 +60,23 @@ def writefraw(x: "N.ndarray", name: str, header: Optional[str] = None) -> None:
     check(lib().pdlgb300_writefraw(C.byref(d), _enc(name), _enc(header)))
 
 
+def _shape_matches(shape, low) -> bool:
+    """PDL::all($pdl->shape == pdl(@ldims)) (FastRaw.pm:338-339) under PDL's
+    broadcasting: pdl() of one number is a 0-dim scalar that every element of
+    the shape is compared with; otherwise two 1-dim ndarrays whose lengths
+    must be equal, or one of them 1 (its element compared with every element
+    of the other), else the comparison itself dies with a broadcast error.
+    The all() of an empty comparison is true."""
+    if len(low) == 1:
+        return all(d == low[0] for d in shape)
+    if len(shape) == len(low):
+        return all(d == l for d, l in zip(shape, low))
+    if len(shape) == 1:
+        return all(shape[0] == l for l in low)
+    raise PDLError(A.EUSERERROR,
+                   f"Mismatched implicit broadcast dimension 0: size {len(shape)} vs. {len(low)}")
+
+
 def gluefraw(x: "N.ndarray", name: str, header: Optional[str] = None) -> None:
     """Append x as one more step of the last dim of the file's ndarray
     (gluefraw, FastRaw.pm:326-346), with the reference's checks."""
@@ -70,9 +87,8 @@ def gluefraw(x: "N.ndarray", name: str, header: Optional[str] = None) -> None:
         raise PDLError(A.EUSERERROR, f"gluefraw: ndarray has type '{x.type}' but file has type '{t}'")
     if len(dims) < 2:
         raise PDLError(A.EUSERERROR, f"gluefraw: header dims needs at least 2 dims, got ({' '.join(map(str, dims))})")
-    low = dims[:-1]
-    shape = tuple(x.dims) + (1,) * max(0, len(low) - x.ndims)
-    if len(x.dims) > len(low) or tuple(shape[: len(low)]) != tuple(low):
+    low = list(dims[:-1])
+    if not _shape_matches(list(x.dims), low):
         raise PDLError(A.EUSERERROR,
                        f"gluefraw: incompatible lower dims, ndarray ({' '.join(map(str, x.dims))}) "
                        f"vs header ({' '.join(map(str, low))})")

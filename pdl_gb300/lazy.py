@@ -111,6 +111,11 @@ class Lazy:
     def __or__(self, o): return Lazy("or2", self, o)
     def __and__(self, o): return Lazy("and2", self, o)
     def __xor__(self, o): return Lazy("xor", self, o)
+    def __rlshift__(self, o): return Lazy("shiftleft", o, self)
+    def __rrshift__(self, o): return Lazy("shiftright", o, self)
+    def __ror__(self, o): return Lazy("or2", o, self)
+    def __rand__(self, o): return Lazy("and2", o, self)
+    def __rxor__(self, o): return Lazy("xor", o, self)
 
     # -- evaluation
     def materialize(self) -> N.ndarray:
@@ -320,6 +325,11 @@ class LazyLeaf:
     def __or__(self, o): return Lazy("or2", self.x, _unwrap(o))
     def __and__(self, o): return Lazy("and2", self.x, _unwrap(o))
     def __xor__(self, o): return Lazy("xor", self.x, _unwrap(o))
+    def __rlshift__(self, o): return Lazy("shiftleft", _unwrap(o), self.x)
+    def __rrshift__(self, o): return Lazy("shiftright", _unwrap(o), self.x)
+    def __ror__(self, o): return Lazy("or2", _unwrap(o), self.x)
+    def __rand__(self, o): return Lazy("and2", _unwrap(o), self.x)
+    def __rxor__(self, o): return Lazy("xor", _unwrap(o), self.x)
 
 
 def _unwrap(o):

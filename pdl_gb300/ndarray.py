@@ -343,6 +343,11 @@ class ndarray:
     def __or__(self, o): return NotImplemented if _deferred(o) else or2(self, o)
     def __and__(self, o): return NotImplemented if _deferred(o) else and2(self, o)
     def __xor__(self, o): return NotImplemented if _deferred(o) else xor(self, o)
+    def __rlshift__(self, o): return NotImplemented if _deferred(o) else shiftleft(self, o, swap=1)
+    def __rrshift__(self, o): return NotImplemented if _deferred(o) else shiftright(self, o, swap=1)
+    def __ror__(self, o): return NotImplemented if _deferred(o) else or2(self, o, swap=1)
+    def __rand__(self, o): return NotImplemented if _deferred(o) else and2(self, o, swap=1)
+    def __rxor__(self, o): return NotImplemented if _deferred(o) else xor(self, o, swap=1)
 
     # -- methods
     def sumover(self, out=None): return sumover(self, out)

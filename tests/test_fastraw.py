@@ -98,3 +98,27 @@ def test_header_type_outside_this_path(tmp_path):
     (tmp_path / "ld.hdr").write_text("11\n1\n2\n")        # long double
     with pytest.raises(P.PDLError, match="not on this path"):
         P.readfraw(str(tmp_path / "ld"))
+
+
+def test_gluefraw_lower_dims_compare_like_the_reference(tmp_path):
+    """FastRaw.pm:338-339 compares $pdl->shape with pdl(@ldims) under
+    broadcasting: a 1-dim x of dims (n) is accepted against lower dims
+    (n, 1) only when n == 1; one lower dim is a scalar every dim is
+    compared with; unequal lengths above 1 are a broadcast error."""
+    base = str(tmp_path / "m")
+    P.writefraw(P.pdl(np.zeros((2, 1, 3))), base)           # dims (3, 1, 2): lower (3, 1)
+    with pytest.raises(P.PDLError, match="incompatible lower dims"):
+        P.gluefraw(P.pdl(np.zeros(3)), base)                 # (3) vs (3 1): 3 != 1
+    P.gluefraw(P.pdl(np.zeros((1, 3))), base)                # (3 1) vs (3 1)
+    ones = str(tmp_path / "ones")
+    P.writefraw(P.pdl(np.zeros((2, 1, 1))), ones)            # lower dims (1, 1)
+    P.gluefraw(P.pdl(np.zeros(1)), ones)                     # (1) broadcasts over (1 1)
+    col = str(tmp_path / "col")
+    P.writefraw(P.pdl(np.zeros((2, 4))), col)                # lower dims (4): a scalar 4
+    with pytest.raises(P.PDLError, match="incompatible lower dims"):
+        P.gluefraw(P.pdl(np.zeros((2, 4))), col)             # (4 2): 2 != 4
+    P.gluefraw(P.pdl(np.zeros(4)), col)
+    cube = str(tmp_path / "cube")
+    P.writefraw(P.pdl(np.zeros((2, 4, 3, 2))), cube)         # lower dims (2, 3, 4)
+    with pytest.raises(P.PDLError, match="Mismatched implicit broadcast dimension 0: size 2 vs. 3"):
+        P.gluefraw(P.pdl(np.zeros((3, 2))), cube)

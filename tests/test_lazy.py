@@ -123,3 +123,35 @@ def test_expression_entry_point_validates_programs():
     assert code and "integer type" in msg
     code, msg = _expr_call("bandover", [a], [("plus", 0, 0)])
     assert code and "not fused" in msg
+
+
+@pytest.mark.parametrize("sym,op", [("<<", "shiftleft"), (">>", "shiftright"),
+                                    ("|", "or2"), ("&", "and2"), ("^", "xor")])
+def test_reversed_bit_and_shift_operators_record_the_swapped_op(sym, op):
+    """An ndarray or a scalar on the left of a bit or shift operator whose
+    right side is deferred records op(left, right), as PDL's overload does
+    with swap set; dims and type equal the eager op's (the oracle's)."""
+    from oracle import oracle as O
+    from pdl_gb300.lazy import LazyLeaf
+    x = P.pdl(np.arange(12, dtype=np.int32).reshape(3, 4))   # dims (4, 3)
+    y = P.pdl(np.arange(4, dtype=np.int64))                   # dims (4,)
+    three = P.pdl(np.int32(3))
+    xx = O.run("mult", [x, x])[0]                             # eager x*x
+    for left, right, eager_left, eager_right in [
+            (y, P.lazy(x), y, x), (3, P.lazy(x), three, x), (y, P.lazy(x) * x, y, xx),
+            (3, P.lazy(x) * x, three, xx)]:
+        e = eval(f"l {sym} r", {"l": left, "r": right})
+        assert isinstance(e, P.Lazy) and e.op == op
+        assert e.b is (right.x if isinstance(right, LazyLeaf) else right)
+        ref = O.run(op, [eager_left, eager_right])[0]
+        assert e.dims == ref.dims and e.type == ref.type
+
+
+@pytest.mark.parametrize("sym,op", [("<<", "shiftleft"), (">>", "shiftright"),
+                                    ("|", "or2"), ("&", "and2"), ("^", "xor")])
+def test_reversed_bit_and_shift_operators_on_ndarrays_are_registered(sym, op):
+    """A scalar on the left of an ndarray's bit or shift operator is the
+    swapped op (Ops.pd's overloads pass swap); the reversed methods exist."""
+    rname = {"<<": "__rlshift__", ">>": "__rrshift__", "|": "__ror__", "&": "__rand__",
+             "^": "__rxor__"}[sym]
+    assert callable(getattr(P.ndarray, rname))

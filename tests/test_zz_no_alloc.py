@@ -67,3 +67,24 @@ def test_noalloc_rejects_too_many_rows_and_host_memory(gpu):
     ho = P.pdl(np.zeros(3))._desc(False)
     e = L.pdlgb300_sumover_noalloc(C.byref(hd), C.byref(ho))
     assert e.error == A.EUSERERROR and b"device-resident" in e.message
+
+
+@pytest.mark.parametrize("t,limit", [("double", 32760), ("float", 32760), ("long", 43680)])
+def test_noalloc_row_limit_boundary(gpu, t, limit):
+    """The documented row limit: (1 MiB - 256) / (2 * (accumulator + 8))
+    rows are accepted and give sumover's result; one more row is refused."""
+    L = A.lib()
+    a = np.ones((limit + 1, 3))
+    a[:, 1] = np.arange(limit + 1) % 7
+    x, dx = _dev(a, t)
+    ref = P.sumover(x).numpy()
+    ok_view = P.from_numpy(a[:limit], t).to_device()
+    dv = ok_view._desc(True)
+    out, dout = _out(P.sumover(ok_view).type, (limit,))
+    A.check(L.pdlgb300_sumover_noalloc(C.byref(dv), C.byref(dout)))
+    A.check(L.pdlgb300_sync())
+    out.storage.fresh = "dev"
+    assert np.array_equal(out.numpy(), ref[:limit])
+    big, dbig = _out(P.sumover(x).type, (limit + 1,))
+    e = L.pdlgb300_sumover_noalloc(C.byref(dx), C.byref(dbig))
+    assert e.error == A.EUSERERROR and f"at most {limit} rows".encode() in e.message
