@@ -92,11 +92,25 @@ __global__ void __launch_bounds__(NT) k_mm_simt(const MMArgs g) {
       badacc[i][j] = false;
     }
 
+  // The reference walks t in tiles of tsiz = 64 / sizeof(T) (a multiple of
+  // BK for every type) and, in bad mode, starts each tile by reading the
+  // partial sum back from c: one equal to c's badvalue is taken as bad and
+  // left as it is (Primitive.pd matmult Code, `if ($ISBADVAR(cc,c))
+  // continue`), including the zero it starts from when that badvalue is 0.
+  constexpr int64_t TSIZ = 64 / sizeof(T);
+  const Bad<T> bc{from_bits<T>(g.cbad), (bool)g.cbad_isnan};
+
   load(0);
   store(0);
   __syncthreads();
   int buf = 0;
   for (int64_t k0 = 0; k0 < g.K; k0 += BK) {
+    if (BAD && k0 % TSIZ == 0) {
+#pragma unroll
+      for (int i = 0; i < TM; i++)
+#pragma unroll
+        for (int j = 0; j < TN; j++) badacc[i][j] |= bc.is(acc[i][j]);
+    }
     const bool more = k0 + BK < g.K;
     if (more) load(k0 + BK);
     const int kend = (int)(g.K - k0 < BK ? g.K - k0 : BK);
@@ -129,7 +143,7 @@ __global__ void __launch_bounds__(NT) k_mm_simt(const MMArgs g) {
       buf ^= 1;
     }
   }
-  const T cbad = from_bits<T>(g.cbad);
+  const T cbad = bc.val;
 #pragma unroll
   for (int i = 0; i < TM; i++) {
     int64_t m = m0 + ty * 4 + (i % 4) + (i / 4) * 64;

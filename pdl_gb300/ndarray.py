@@ -446,7 +446,8 @@ def pdl(x, type=None) -> ndarray:
         if arr.dtype.kind in "iu" and arr.dtype == np.int64 and type is None and not isinstance(x, np.ndarray):
             arr = arr.astype(np.float64)  # PDL's pdl(...) of Perl numbers is double
         arr = _c_order(arr)
-    t = _NP_TO_TYPE[arr.dtype]
+    # a named type wins over the numpy dtype (indx and longlong share int64)
+    t = type_code(type) if type is not None else _NP_TO_TYPE[arr.dtype]
     flat = arr.reshape(-1).view(np.uint8) if arr.size else np.zeros(1, np.uint8)
     st = Storage(arr.nbytes, host=flat)
     return ndarray(st, t, arr.shape[::-1])
@@ -458,12 +459,12 @@ def from_numpy(arr: np.ndarray, type=None) -> ndarray:
 
 def zeroes(type, *dims) -> ndarray:
     t = type_code(type)
-    return from_numpy(np.zeros(tuple(dims)[::-1], dtype=NP_DTYPES[t]))
+    return from_numpy(np.zeros(tuple(dims)[::-1], dtype=NP_DTYPES[t]), t)
 
 
 def ones(type, *dims) -> ndarray:
     t = type_code(type)
-    return from_numpy(np.ones(tuple(dims)[::-1], dtype=NP_DTYPES[t]))
+    return from_numpy(np.ones(tuple(dims)[::-1], dtype=NP_DTYPES[t]), t)
 
 
 def sequence(type, *dims) -> ndarray:
