@@ -1439,18 +1439,21 @@ int oracle_run(const char *opname, pdlgb300_ndarray **pdls_in, const int64_t *ot
         return set_err(&e, "%s: output %s has type %s, needs %s", d->name,
                        d->par_names[j], oracle_type_name(p->datatype),
                        oracle_type_name(want));
+      /* pdl_get_convertedpdl (pdlapi.c:141-165) makes a converttypei child:
+       * its CHILD parameter is PDL_PARAM_ISIGNORE, so the child keeps
+       * has_badvalue = 0 (pdlapi.c:1240-1258) and its badvalue is the new
+       * type's default; COPYCONVERT maps the parent's bad elements to it
+       * (pdlconv.c:163-174). */
       void *cp = converted_copy(p, want, bvalflag && (p->state & PDLGB300_BADVAL));
       pdlgb300_value nb = default_bad(want);
-      if (p->has_badvalue) convert_elem(p->datatype, &p->badvalue.value, want, &nb);
       tofree[j] = cp;
       int64_t dims[PDLGB300_MAXDIMS];
       memcpy(dims, p->dims, sizeof dims);
       int nd = p->ndims;
       uint32_t st = p->state;
-      int hb = p->has_badvalue;
       oracle_ndarray_init(p, want, nd, dims, cp, NULL);
       p->state = st;
-      p->has_badvalue = hb;
+      p->has_badvalue = 0;
       p->badvalue.type = want;
       p->badvalue.value = nb;
       /* strides changed: recompute the broadcast increments */

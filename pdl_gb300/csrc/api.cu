@@ -964,10 +964,19 @@ pdlgb300_error dispatch_reduce(RunCtx &c, int redop) {
     lc.kind = 1;  // thread per row, coalesced across rows
     lc.block = 128;
     lc.grid = (int)std::min<int64_t>((a.rows + 127) / 128, (int64_t)nsm * 64);
-  } else if (a.n * (int64_t)isz <= 32768) {
+  } else if (a.n * (int64_t)isz <= 32768 &&
+             (a.rows * 32 >= (int64_t)nsm * 1536 || a.n * (int64_t)isz <= 4096)) {
     a.group = 32;  // rows up to 32 KiB: a warp per row, 8 rows per block
     lc.block = 256;
     lc.grid = (int)std::min<int64_t>((a.rows + 7) / 8, (int64_t)1 << 30);
+  } else if (a.n * (int64_t)isz <= 32768) {
+    // too few rows to fill the SMs a warp each: a block per row, 128 bytes
+    // per thread, so a row is in flight in one round trip and the blocks
+    // spread evenly over the SMs
+    const int64_t want = a.n * (int64_t)isz / 128;
+    a.group = want >= 256 ? 256 : want >= 128 ? 128 : 64;
+    lc.block = a.group;
+    lc.grid = (int)std::min<int64_t>(a.rows, (int64_t)1 << 30);
   } else {
     a.group = a.n >= 16384 ? 256 : 128;
     lc.block = a.group;
@@ -990,8 +999,17 @@ pdlgb300_error dispatch_reduce(RunCtx &c, int redop) {
     lc.grid = (int)std::min<int64_t>(units, (int64_t)1 << 30);
   }
   void *scratch = nullptr;
-  // floating products (row kernel): per row, the first good exact zero
   const int dtin = c.v[0].datatype;
+  // floating products: the reference's sequential product with its early
+  // exit, by the prefix/suffix kernel (rows up to 2^20 elements)
+  if (lc.kind == 0 && a.n <= PROD_SEQ_MAXN &&
+      (redop == R_DPROD || (redop == R_PROD && (dtin == PDLGB300_F || dtin == PDLGB300_D)))) {
+    const int64_t S = std::min<int64_t>(a.n, redop == R_PROD && dtin == PDLGB300_F ? 4096 : 2048);
+    tl_info.grid = (a.rows + 31) / 32;
+    return launch_prod_seq(redop, dtin, a, S, g_stream);
+  }
+  // floating products of longer rows (row kernel): per row, the first good
+  // exact zero
   const bool zfix = lc.kind == 0 && (redop == R_DPROD ||
                                      (redop == R_PROD && (dtin == PDLGB300_F || dtin == PDLGB300_D)));
   if (a.nsplit > 1 || zfix) {

@@ -80,6 +80,10 @@ pdlgb300_error launch_expr_reduce(int redop, int dt, const ExprArgs &g, const Re
                                   int grid, int block, cudaStream_t s);
 pdlgb300_error launch_red_sum(int op, int in_dt, RedArgs args, const RedLaunch &lc,
                               cudaStream_t s);
+// Floating prodover/dprodover with the reference's early exit (prod_seq.cu):
+// the first S elements of each row sequentially, then the rest.
+constexpr int64_t PROD_SEQ_MAXN = (int64_t)1 << 20;
+pdlgb300_error launch_prod_seq(int op, int in_dt, const RedArgs &a, int64_t S, cudaStream_t s);
 pdlgb300_error launch_red_prod(int op, int in_dt, RedArgs args, const RedLaunch &lc,
                                cudaStream_t s);
 pdlgb300_error launch_red_minmax(int op, int in_dt, RedArgs args, const RedLaunch &lc,

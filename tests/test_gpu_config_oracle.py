@@ -5,8 +5,9 @@ against another GPU path.
 * float64 (4096, 2048) uniform[-1,1) seed 1 (Ufunc family): every op of the
   family against the oracle over all 2048 rows.  minimum/maximum and their
   indices bit-exact; sums, averages and running sums within the reference's
-  own bound for a sequential sum, (n+2)*eps*sum|a|; prodover equal (every
-  row's running product underflows to zero).
+  own bound for a sequential sum, (n+2)*eps*sum|a|; prodover bit for bit,
+  the sign of each zero included (the reference stops at the first zero of
+  its running product, lib/PDL/Ufunc.pd:107).
 * float32 (65536, 4096) plus one row of 2^27, lognormal(0,4) magnitudes,
   random sign, 1 % BAD, seed 7 (accuracy stress): sumover, average,
   cumusumover, dsumover and dcumusumover on 64 sampled rows of the matrix
@@ -54,12 +55,12 @@ def test_c1_family_against_the_oracle(gpu, c1, op):
     exp = O.run(op, [h], nthreads=NTH)[0]
     assert got.type == exp.type and got.dims == exp.dims and got.badflag() == exp.badflag()
     g, e = got.numpy(), exp.numpy()
-    if op in ("minimum", "maximum", "minimum_ind", "maximum_ind"):
-        assert np.array_equal(g.view(np.uint64), e.view(np.uint64))   # bit for bit
-        return
-    if op == "prodover":
-        # every row's running product underflows to zero before the end
-        assert np.array_equal(g, e) and np.all(e == 0)
+    if op in ("minimum", "maximum", "minimum_ind", "maximum_ind", "prodover"):
+        # bit for bit (prodover: every row's running product underflows to a
+        # signed zero before the end; the sign is the product's at that point)
+        assert np.array_equal(g.view(np.uint64), e.view(np.uint64))
+        if op == "prodover":
+            assert np.all(e == 0)
         return
     absa = np.abs(a)
     scale = np.cumsum(absa, -1) if op == "cumusumover" else absa.sum(-1)

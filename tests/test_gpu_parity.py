@@ -424,6 +424,72 @@ def test_prodover_stops_at_first_zero(gpu, op, t):
             assert np.array_equal(np.signbit(g[zero]), np.signbit(e[zero])), f"{op} {t}: sign of 0"
 
 
+@pytest.mark.parametrize("t", FLOAT_TYPES)
+@pytest.mark.parametrize("op", ["prodover", "dprodover"])
+def test_products_leaving_the_normal_range_are_the_references(gpu, op, t):
+    """Rows whose running product overflows, underflows (to a subnormal and
+    to zero), or comes back into range, with zeros, infs, NaNs and bad
+    values before and after the sequential prefix (2048 or 4096 elements):
+    the result is the reference's loop's, bit for bit (NaN positions
+    equal, zeros' signs equal)."""
+    dt = NP_DTYPES[type_code(t)]
+    rng = seeded(("leave", op, t))
+    big = 1e30 if t == "float" else 1e200
+    rows = []
+    for n in (100, 3000, 5000, 9000):
+        base = rng.uniform(0.9, 1.1, n) * np.where(rng.random(n) < 0.5, -1, 1)
+        for k in range(6):
+            r = base.copy()
+            p = int(rng.integers(0, n))
+            if k == 0:
+                r[p], r[min(p + 1, n - 1)] = big, big          # overflow, stays inf
+            elif k == 1:
+                r[p], r[min(p + 1, n - 1)] = 1 / big, 1 / big  # underflow to 0 (stops)
+            elif k == 2:
+                r[p] = big
+                r[min(p + 3, n - 1)] = 1 / big                 # back in range
+            elif k == 3:
+                r[p] = 0.0
+                r[min(p + 5, n - 1)] = np.inf                  # zero then inf: stays 0
+            elif k == 4:
+                r[p], r[min(p + 1, n - 1)] = big, big
+                r[min(p + 9, n - 1)] = 0.0                     # inf then 0: NaN
+            else:
+                r[:] = rng.uniform(-1, 1, n)                   # drifts to a signed 0
+            rows.append(r)
+    width = max(len(r) for r in rows)
+    for r in rows:
+        a = np.ones((1, width))
+        a[0, :len(r)] = r
+        x = to_pdl(a.astype(dt), t)
+        got, exp = _run_both(op, [x])
+        g, e = got.numpy(), exp.numpy()
+        what = f"{op} {t} n={len(r)}"
+        assert np.array_equal(np.isnan(g), np.isnan(e)), what
+        fin = ~np.isnan(e)
+        bits = np.uint64 if g.dtype.itemsize == 8 else np.uint32
+        if not np.isfinite(e[fin]).all() or (e[fin] == 0).any():
+            assert np.array_equal(g[fin].view(bits), e[fin].view(bits)), f"{what}: {g} {e}"
+        else:
+            np.testing.assert_allclose(g[fin], e[fin], rtol=(width + 2) * EPS["double" if op == "dprodover" else t])
+    # the same rows together, and with 5 % bad values
+    a = np.ones((len(rows), width))
+    for i, r in enumerate(rows):
+        a[i, :len(r)] = r
+    a = a.astype(dt)
+    for badfrac in (0.0, 0.05):
+        b = a.copy()
+        if badfrac:
+            b[rng.random(b.shape) < badfrac] = P.default_badvalue(type_code(t))
+        x = to_pdl(b, t, badflag=bool(badfrac))
+        got, exp = _run_both(op, [x])
+        g, e = got.numpy(), exp.numpy()
+        assert np.array_equal(np.isnan(g), np.isnan(e))
+        special = ~np.isnan(e) & (~np.isfinite(e) | (e == 0))
+        bits = np.uint64 if g.dtype.itemsize == 8 else np.uint32
+        assert np.array_equal(g[special].view(bits), e[special].view(bits))
+
+
 def test_prodover_zero_in_bad_and_integer_rows(gpu):
     rng = seeded(31)
     a, bad = rand_array(rng, "double", (4, 5000), 0.9, 1.1, bad_frac=0.1)
