@@ -269,6 +269,7 @@ def run_ours(args, rank, world):
         result["matmult"] = bench_matmult(args, P, torch, stream, bf16, peak_kind)
     if args.secondary and rank == 0:
         result["fused_c2"] = bench_c2(args, P, torch, stream)
+        result["adjoint_c4"] = bench_c4(args, P, torch, stream)
         result["inner_c3"] = bench_inner(args, P, torch, stream, hbm)
         result["expr"] = bench_expr(args, P, torch, stream, hbm)
         result["sort"] = bench_sort(args, P, torch, stream, hbm)
@@ -554,6 +555,100 @@ def bench_c2(args, P, torch, stream):
     return out
 
 
+def c4_inputs():
+    rng = np.random.default_rng(6)
+    X = (0.1 * rng.standard_normal((8192, 512))).astype(np.float32)   # PDL X(t=512, h=8192)
+    Wm = (0.1 * rng.standard_normal((512, 256))).astype(np.float32)   # PDL W(w=256, t=512)
+    bias = (0.1 * rng.standard_normal(256)).astype(np.float32)        # PDL bias(w=256)
+    return X, Wm, bias
+
+
+def bench_c4(args, P, torch, stream):
+    """Adjoint workload: L = sumover(sumover((matmult(X,W) + bias)**2)) / 8192,
+    X float32 dims (512, 8192), W (256, 512), bias (256), N(0, 0.1), seed 6.
+    Forward through the ops, backward through the hand-written adjoint calls
+    (intermediates recomputed, nothing stored but the inputs and the
+    forward's outputs), gradients into preallocated buffers.  Accuracy: FP64
+    central finite differences (eps 1e-3) on 64 coordinates (24 of X, 24 of
+    W, 16 of bias; the loss change of one coordinate summed from the terms it
+    changes), and the hand-derived FP64 gradient everywhere."""
+    X, Wm, bias = c4_inputs()
+    x, w, b = P.pdl(X).to_device(), P.pdl(Wm).to_device(), P.pdl(bias).to_device()
+    Y = P.matmult(x, w)
+    Z = P.plus(Y, b)
+    S = P.mult(Z, Z)
+    s1 = P.sumover(S)
+    L = P.sumover(s1)
+    gL = P.pdl(np.array(1.0 / 8192, np.float32)).to_device()
+    g_s1 = P.sumover_bwd(gL, s1)
+    g_S = P.sumover_bwd(g_s1, S)
+    gz1, gz2 = P.mult_bwd(g_S, Z, Z)
+    g_Z = P.plus(gz1, gz2)
+    g_Y, g_b = P.plus_bwd(g_Z, Y, b)
+    g_X, g_W = P.matmult_bwd(g_Y, x, w)
+    P.sync()
+
+    def fwd():
+        P.matmult(x, w, Y)
+        P.plus(Y, b, Z)
+        P.mult(Z, Z, S)
+        P.sumover(S, s1)
+        P.sumover(s1, L)
+
+    def bwd():
+        P.sumover_bwd(gL, s1, out=g_s1)
+        P.sumover_bwd(g_s1, S, out=g_S)
+        P.mult_bwd(g_S, Z, Z, out=(gz1, gz2))
+        P.plus(gz1, gz2, g_Z)
+        P.plus_bwd(g_Z, Y, b, out=(g_Y, g_b))
+        P.matmult_bwd(g_Y, x, w, out=(g_X, g_W))
+
+    reps = args.mm_steps + 7
+    ms_f = time_op(torch, stream, fwd, reps)
+    ms_b = time_op(torch, stream, bwd, reps)
+    ms_t = time_op(torch, stream, lambda: (fwd(), bwd()), reps)
+    fwd_flop = 2.0 * 512 * 256 * 8192
+    bwd_flop = 2 * fwd_flop
+    # accuracy against FP64
+    gX, gW, gb = g_X.numpy().astype(np.float64), g_W.numpy().astype(np.float64), g_b.numpy().astype(np.float64)
+    X64, W64, b64 = X.astype(np.float64), Wm.astype(np.float64), bias.astype(np.float64)
+    Z64 = X64 @ W64 + b64                                    # (h, w)
+    gZ = 2.0 * Z64 / 8192.0
+    ref = {"X": gZ @ W64.T, "W": X64.T @ gZ, "bias": gZ.sum(0)}
+    got = {"X": gX, "W": gW, "bias": gb}
+    normwise = {k: float(np.max(np.abs(got[k] - ref[k])) / np.max(np.abs(ref[k]))) for k in ref}
+    rng = np.random.default_rng(60)
+    eps, fd_err = 1e-3, 0.0
+
+    def dloss(rows_old, rows_new):
+        return float(((rows_new * rows_new).sum() - (rows_old * rows_old).sum()) / 8192.0)
+    for name, n in [("X", 24), ("W", 24), ("bias", 16)]:
+        arr = {"X": X64, "W": W64, "bias": b64}[name]
+        for i in rng.choice(arr.size, n, replace=False):
+            if name == "X":
+                h, t = divmod(int(i), 512)
+                old = Z64[h]
+                lp, lm = dloss(old, old + eps * W64[t]), dloss(old, old - eps * W64[t])
+            elif name == "W":
+                t, wv = divmod(int(i), 256)
+                old = Z64[:, wv]
+                lp, lm = dloss(old, old + eps * X64[:, t]), dloss(old, old - eps * X64[:, t])
+            else:
+                old = Z64[:, int(i)]
+                lp, lm = dloss(old, old + eps), dloss(old, old - eps)
+            fd = (lp - lm) / (2 * eps)
+            g = float(got[name].reshape(-1)[i])
+            fd_err = max(fd_err, abs(g - fd) / max(abs(fd), 1e-4))
+    return {"config": "L = sumover(sumover((matmult(X,W)+bias)**2))/8192, X float32 (512,8192), "
+                      "W (256,512), bias (256), N(0,0.1) seed 6",
+            "fwd_ms": ms_f, "bwd_ms": ms_b, "fwd_bwd_ms": ms_t,
+            "fwd_tflops": fwd_flop / (ms_f * 1e-3) / 1e12,
+            "bwd_tflops": bwd_flop / (ms_b * 1e-3) / 1e12,
+            "max_rel_err_vs_fp64_central_fd_64_coords": fd_err,
+            "max_normwise_err_vs_fp64_gradient": normwise,
+            "kernels": "k_mm_tc_bf16x6 (matmult and its adjoints), k_biop, k_red_rows, k_unb_*"}
+
+
 def bench_inner(args, P, torch, stream, hbm):
     """Config 3 inner: float64 a, b dims (4096, 65536), U[-1,1) -> 65536."""
     cols = args.inner_cols
@@ -715,6 +810,8 @@ def main():
                     help="time only the sort-based workload and print its object")
     ap.add_argument("--family-only", action="store_true",
                     help="time only the float64 family (--ops) and print its object")
+    ap.add_argument("--c4-only", action="store_true",
+                    help="time only the adjoint workload and print its object")
     ap.add_argument("--c2-only", action="store_true",
                     help="time only the fused sumover(a*b+a) workload and print its object")
     ap.add_argument("--c2-types", default="int32,float32_bad",
@@ -728,13 +825,13 @@ def main():
             return 0
         print(json.dumps(run_reference(args, rank, world)))
         return 0
-    if args.expr_only or args.sort_only or args.family_only or args.c2_only:
+    if args.expr_only or args.sort_only or args.family_only or args.c2_only or args.c4_only:
         import torch
         import pdl_gb300 as P
         stream = torch.cuda.current_stream()
         P.set_stream(stream.cuda_stream)
-        if args.c2_only:
-            print(json.dumps(bench_c2(args, P, torch, stream)))
+        if args.c2_only or args.c4_only:
+            print(json.dumps((bench_c2 if args.c2_only else bench_c4)(args, P, torch, stream)))
             return 0
         fn = bench_expr if args.expr_only else bench_sort if args.sort_only else run_family
         print(json.dumps(fn(args, P, torch, stream, peaks()[0])))

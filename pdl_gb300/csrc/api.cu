@@ -964,19 +964,13 @@ pdlgb300_error dispatch_reduce(RunCtx &c, int redop) {
     lc.kind = 1;  // thread per row, coalesced across rows
     lc.block = 128;
     lc.grid = (int)std::min<int64_t>((a.rows + 127) / 128, (int64_t)nsm * 64);
-  } else if (a.n * (int64_t)isz <= 32768 &&
-             (a.rows * 32 >= (int64_t)nsm * 1536 || a.n * (int64_t)isz <= 4096)) {
-    a.group = 32;  // rows up to 32 KiB: a warp per row, 8 rows per block
+  } else if (a.n * (int64_t)isz <= 32768) {
+    // rows up to 32 KiB: a warp per row, 8 rows per block (a block per row
+    // with 128 bytes per thread measured slower on the float64 (4096, 2048)
+    // family: its 256-thread row merges cost more than the occupancy gained)
+    a.group = 32;
     lc.block = 256;
     lc.grid = (int)std::min<int64_t>((a.rows + 7) / 8, (int64_t)1 << 30);
-  } else if (a.n * (int64_t)isz <= 32768) {
-    // too few rows to fill the SMs a warp each: a block per row, 128 bytes
-    // per thread, so a row is in flight in one round trip and the blocks
-    // spread evenly over the SMs
-    const int64_t want = a.n * (int64_t)isz / 128;
-    a.group = want >= 256 ? 256 : want >= 128 ? 128 : 64;
-    lc.block = a.group;
-    lc.grid = (int)std::min<int64_t>(a.rows, (int64_t)1 << 30);
   } else {
     a.group = a.n >= 16384 ? 256 : 128;
     lc.block = a.group;
@@ -2195,6 +2189,34 @@ pdlgb300_error mm_grad(pdlgb300_ndarray p, pdlgb300_ndarray q, pdlgb300_ndarray 
     pdlgb300_ndarray out = *target;
     pdlgb300_ndarray *qq[3] = {&p, &q, &out};
     return run_impl(&VT[O_MATMULT], qq, nullptr);
+  }
+  // Every batch dim summed away, and in both operands each batch dim's
+  // increment continues the contraction's (inc(b1) = inc(k) * K, ...): the
+  // batch is part of the contraction, c(w, h) = sum over (k, b) of
+  // p(k, h, b) q(w, k, b), one matmult of contraction K * B into the target.
+  {
+    bool fold = p.ndims >= 2 && q.ndims >= 2 && p.ndims == q.ndims && full.ndims > 2;
+    for (int k = 2; k < full.ndims && fold; k++)
+      fold = (k >= target->ndims || target->dims[k] == 1) && p.dims[k] == full.dims[k] &&
+             q.dims[k] == full.dims[k];
+    for (int k = 2; k < target->ndims && fold; k++) fold = k < full.ndims && target->dims[k] == 1;
+    int64_t K = p.dims[0], ip = p.incs[0], iq = q.incs[1];
+    for (int k = 2; k < full.ndims && fold; k++) {
+      if (full.dims[k] == 1) continue;
+      fold = p.incs[k] == ip * K && q.incs[k] == iq * K && ip != 0 && iq != 0;
+      K *= full.dims[k];
+    }
+    if (fold && K != p.dims[0]) {
+      pdlgb300_ndarray pf = p, qf = q, out = *target;
+      pf.ndims = 2;
+      pf.dims[0] = K;
+      qf.ndims = 2;
+      qf.dims[1] = K;
+      out.ndims = 2;
+      for (int k = target->ndims; k < 2; k++) { out.dims[k] = 1; out.incs[k] = 0; }
+      pdlgb300_ndarray *qq[3] = {&pf, &qf, &out};
+      return run_impl(&VT[O_MATMULT], qq, nullptr);
+    }
   }
   pdlgb300_ndarray tmp;
   pdlgb300_ndarray_null(&tmp);

@@ -237,6 +237,8 @@ struct UnbArgs {  // out(o) = sum over r of f(in(o, r))
   Loop Lo;                         // output index space: pdl 0 x, 1 y, 2 out
   Loop Lr;                         // reduced index space: pdl 0 x, 1 y
   double scale;
+  int nsplit;                      // r splits (column kernel), set by the launcher
+  void *partials;                  // per (split, output) partial sums when nsplit > 1
 };
 pdlgb300_error launch_unbroadcast(int dt, const UnbArgs &g, cudaStream_t s);
 }  // namespace pg

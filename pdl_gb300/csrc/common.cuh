@@ -130,6 +130,26 @@ template <class T> __device__ __forceinline__ T op_add(T a, T b) {
   if constexpr (std::is_floating_point_v<T>) return rn_add(a, b); else return wadd(a, b);
 }
 
+// Bit operations on the raw bits of a double, opaque to the compiler: a
+// mask of the sign bit or a shifted zero test on bits that came from a
+// double is otherwise rewritten into fabs / an FP64 compare, which run on
+// GB300's narrow FP64 pipe.
+__device__ __forceinline__ uint64_t and_b64(uint64_t a, uint64_t m) {
+  uint64_t r;
+  asm("and.b64 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(m));
+  return r;
+}
+__device__ __forceinline__ uint32_t hi_b32(uint64_t a) {
+  uint32_t lo, hi;
+  asm("mov.b64 {%0, %1}, %2;" : "=r"(lo), "=r"(hi) : "l"(a));
+  return hi;
+}
+__device__ __forceinline__ bool zero_bits64(uint64_t a) {  // +0 or -0
+  uint32_t lo, hi;
+  asm("mov.b64 {%0, %1}, %2;" : "=r"(lo), "=r"(hi) : "l"(a));
+  return ((hi << 1) | lo) == 0;
+}
+
 // PDL_ISBAD2: NaN badvalue => isnan, else equality.
 template <class T> struct Bad {
   T val;

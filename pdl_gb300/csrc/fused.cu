@@ -141,23 +141,71 @@ __global__ void __launch_bounds__(FT) k_fused_outer(const FusedArgs g) {
           xd[x] = g.fd && bd.is(dv[x]);
           xb[x] = g.fb && bb.is(bv[x]);
         }
-        auto pairs = [&](auto tnan) {
-          constexpr bool TN = decltype(tnan)::value;
-          auto isbt = [&](T v) { return TN ? (v != v) : (v == tbad); };
+        // Fast path: a bad a, b or d makes the pair's u bad (skipped); a
+        // good pair is skipped only when t = a*b or u = t + d equals the
+        // intermediates' badvalue.  Bounds from this step's good values
+        // rule that out: |t| <= max|a| max|b| and |u| <= |t| + max|d|
+        // (rounded up), below |badvalue|; with a NaN badvalue, finite good
+        // values give finite-or-inf t and u, never NaN.  Then bad a and d
+        // are zeroed once per value and a pair costs a product, a sum, a
+        // select and the compensated add.
+        bool ka[4];
+        T a0[4], d0[4], b0[4];
+        float ma = 0.0f, mb = 0.0f, md = 0.0f;
+        bool fin = true;
+#pragma unroll
+        for (int x = 0; x < 4; x++) {
+          ka[x] = xa[x] || xd[x];
+          a0[x] = ka[x] ? (T)0 : av[x];
+          d0[x] = ka[x] ? (T)0 : dv[x];
+          b0[x] = xb[x] ? (T)0 : bv[x];
+          ma = fmaxf(ma, fabsf((float)a0[x]));
+          md = fmaxf(md, fabsf((float)d0[x]));
+          mb = fmaxf(mb, fabsf((float)b0[x]));
+          if constexpr (std::is_floating_point_v<T>)
+            fin = fin && isfinite(a0[x]) && isfinite(d0[x]) && isfinite(b0[x]);
+        }
+        bool fast;
+        if constexpr (std::is_floating_point_v<T>) {
+          if (bt.isnan_) {
+            fast = fin;
+          } else {
+            // (float bounds of double values are rounded to nearest: the
+            // margin of 2^-20 covers that and the products' own rounding)
+            const float bound = __fmaf_ru(ma, mb, md) * (1.0f + 0x1p-20f);
+            fast = fin && bound < fabsf((float)tbad);
+          }
+        } else {
+          fast = false;
+        }
+        if (fast) {
 #pragma unroll
           for (int y = 0; y < 4; y++)
 #pragma unroll
             for (int x = 0; x < 4; x++) {
-              const T t = (xa[x] || xb[y]) ? tbad : op_mul<T>(av[x], bv[y]);
-              const T u = ((ft && isbt(t)) || xd[x]) ? ubad : op_add<T>(t, dv[x]);
-              if (!(fu && isbt(u))) {
-                FA::add(acc[y][x], u);
-                cnt[y][x]++;
-              }
+              const T u = op_add<T>(op_mul<T>(a0[x], b0[y]), d0[x]);
+              FA::add(acc[y][x], xb[y] ? (T)0 : u);
+              cnt[y][x] += !(ka[x] || xb[y]);
             }
-        };
-        if (bt.isnan_) pairs(std::true_type{});
-        else pairs(std::false_type{});
+        } else {
+          auto pairs = [&](auto tnan) {
+            constexpr bool TN = decltype(tnan)::value;
+            auto isbt = [&](T v) { return TN ? (v != v) : (v == tbad); };
+#pragma unroll
+            for (int y = 0; y < 4; y++)
+#pragma unroll
+              for (int x = 0; x < 4; x++) {
+                const T t = (xa[x] || xb[y]) ? tbad : op_mul<T>(av[x], bv[y]);
+                const T u = ((ft && isbt(t)) || xd[x]) ? ubad : op_add<T>(t, dv[x]);
+                if (!(fu && isbt(u))) {
+                  FA::add(acc[y][x], u);
+                  cnt[y][x]++;
+                }
+              }
+          };
+          if (bt.isnan_) pairs(std::true_type{});
+          else pairs(std::false_type{});
+        }
       } else {
 #pragma unroll
         for (int y = 0; y < 4; y++)

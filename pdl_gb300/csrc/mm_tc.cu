@@ -305,26 +305,85 @@ struct SplitArgs {
   int p;
 };
 
+// The limbs of one float32: x0 = rn(x), x1 = rn(x - x0), x2 = rn(x - x0 - x1).
+template <int LIMBS>
+__device__ __forceinline__ void split1(float x, __nv_bfloat16 (&h)[3]) {
+  h[0] = __float2bfloat16_rn(x);
+  const float r1 = __fsub_rn(x, __bfloat162float(h[0]));
+  h[1] = __float2bfloat16_rn(r1);
+  h[2] = LIMBS == 3 ? __float2bfloat16_rn(__fsub_rn(r1, __bfloat162float(h[1])))
+                    : __float2bfloat16_rn(0.f);
+}
+
+// Rows whose k is contiguous (s_k == 1): a thread splits 8 consecutive k of
+// one row and writes 16 bytes per limb; k past K (the padding) is zero.
 template <int LIMBS>
 __global__ void __launch_bounds__(256) k_split(const SplitArgs g) {
-  const int64_t per = g.rows * g.Kp, total = per * g.nb;
+  const int64_t kc = g.Kp / 8, nrow = g.rows * g.nb, total = nrow * kc;
+  const int64_t per_limb = g.nb * g.rows * g.Kp;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
        i += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t z = i / per, r = (i - z * per) / g.Kp, k = i % g.Kp;
-    float x = 0.f;
-    if (k < g.K) {
-      int64_t offs[MAXP];
-      loop_offsets(g.L, z, offs);
-      x = g.src[offs[g.p] + r * g.s_row + k * g.s_k];
+    const int64_t rr = i / kc, k0 = (i - rr * kc) * 8;
+    const int64_t z = rr / g.rows, r = rr - z * g.rows;
+    int64_t offs[MAXP];
+    loop_offsets(g.L, z, offs);
+    const float *src = g.src + offs[g.p] + r * g.s_row;
+    float x[8];
+    if (k0 + 8 <= g.K && ((uintptr_t)(src + k0) & 15) == 0) {
+      const float4 u = __ldcs(reinterpret_cast<const float4 *>(src + k0));
+      const float4 v = __ldcs(reinterpret_cast<const float4 *>(src + k0 + 4));
+      x[0] = u.x; x[1] = u.y; x[2] = u.z; x[3] = u.w;
+      x[4] = v.x; x[5] = v.y; x[6] = v.z; x[7] = v.w;
+    } else {
+#pragma unroll
+      for (int e = 0; e < 8; e++) x[e] = k0 + e < g.K ? src[k0 + e] : 0.f;
     }
-    __nv_bfloat16 h0 = __float2bfloat16_rn(x);
-    float r1 = __fsub_rn(x, __bfloat162float(h0));
-    __nv_bfloat16 h1 = __float2bfloat16_rn(r1);
-    g.dst[i] = h0;
-    g.dst[total + i] = h1;
-    if (LIMBS == 3) {
-      float r2 = __fsub_rn(r1, __bfloat162float(h1));
-      g.dst[2 * total + i] = __float2bfloat16_rn(r2);
+    __align__(16) __nv_bfloat16 o[3][8];
+#pragma unroll
+    for (int e = 0; e < 8; e++) {
+      __nv_bfloat16 h[3];
+      split1<LIMBS>(x[e], h);
+#pragma unroll
+      for (int l = 0; l < LIMBS; l++) o[l][e] = h[l];
+    }
+    __nv_bfloat16 *d = g.dst + rr * g.Kp + k0;
+#pragma unroll
+    for (int l = 0; l < LIMBS; l++)
+      *reinterpret_cast<uint4 *>(d + l * per_limb) = *reinterpret_cast<const uint4 *>(o[l]);
+  }
+}
+
+// Rows whose k is strided (the b(w, t) operand, w contiguous): 32 x 32
+// tiles through shared memory, read along the rows, written along k.
+template <int LIMBS>
+__global__ void __launch_bounds__(256) k_split_t(const SplitArgs g) {
+  __shared__ float t[32][33];
+  const int64_t rt = (g.rows + 31) / 32, kt = g.Kp / 32;
+  const int64_t tiles = g.nb * rt * kt;
+  const int64_t per_limb = g.nb * g.rows * g.Kp;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 8 warps
+  for (int64_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+    const int64_t z = tile / (rt * kt), rem = tile - z * rt * kt;
+    const int64_t r0 = (rem / kt) * 32, k0 = (rem % kt) * 32;
+    int64_t offs[MAXP];
+    loop_offsets(g.L, z, offs);
+    const float *src = g.src + offs[g.p];
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < 4; j++) {  // k = k0 + ty + 8j, row = r0 + tx (coalesced along rows)
+      const int64_t k = k0 + ty + 8 * j, r = r0 + tx;
+      t[ty + 8 * j][tx] = (k < g.K && r < g.rows) ? src[r * g.s_row + k * g.s_k] : 0.f;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < 4; j++) {  // row = r0 + ty + 8j, k = k0 + tx (coalesced along k)
+      const int64_t r = r0 + ty + 8 * j;
+      if (r >= g.rows) continue;
+      __nv_bfloat16 h[3];
+      split1<LIMBS>(t[tx][ty + 8 * j], h);
+      __nv_bfloat16 *d = g.dst + (z * g.rows + r) * g.Kp + k0 + tx;
+#pragma unroll
+      for (int l = 0; l < LIMBS; l++) d[l * per_limb] = h[l];
     }
   }
 }
@@ -381,17 +440,28 @@ pdlgb300_error tc_typed(const MMArgs &g, cudaStream_t s) {
   errp = (int *)(((uintptr_t)errp + 15) & ~(uintptr_t)15);
   cudaMemsetAsync(errp, 0, sizeof(int), s);
   const int nsm = pgh::num_sms();
+  // each operand's limbs: k contiguous -> k_split, else the transposing k_split_t
+  auto split = [&](const SplitArgs &sg, int64_t rows, int64_t nb, int64_t sk) {
+    if (sk == 1) {
+      const int64_t n8 = nb * rows * (Kp / 8);
+      const int64_t grid = std::min<int64_t>((n8 + 255) / 256, (int64_t)nsm * 64);
+      k_split<LIMBS><<<(int)grid, 256, 0, s>>>(sg);
+      pgh::record_kernel("k_split", grid, 256);
+    } else {
+      const int64_t tiles = nb * ((rows + 31) / 32) * (Kp / 32);
+      const int64_t grid = std::min<int64_t>(tiles, (int64_t)nsm * 16);
+      k_split_t<LIMBS><<<(int)grid, 256, 0, s>>>(sg);
+      pgh::record_kernel("k_split_t", grid, 256);
+    }
+  };
   SplitArgs sa{reinterpret_cast<const float *>(g.a), al, g.M, g.K, Kp, nA, g.a_m, g.a_k, g.L, 0};
-  int64_t ga = std::min<int64_t>((nA * g.M * Kp + 255) / 256, (int64_t)nsm * 32);
-  k_split<LIMBS><<<(int)ga, 256, 0, s>>>(sa);
+  split(sa, g.M, nA, g.a_k);
   SplitArgs sb{reinterpret_cast<const float *>(g.b), bl, g.N, g.K, Kp, nB, g.b_n, g.b_k, g.L, 1};
-  int64_t gb = std::min<int64_t>((nB * g.N * Kp + 255) / 256, (int64_t)nsm * 32);
-  k_split<LIMBS><<<(int)gb, 256, 0, s>>>(sb);
+  split(sb, g.N, nB, g.b_k);
   if (!pgh::cuda_check(cudaGetLastError(), &e, "k_split")) {
     cudaFreeAsync(scratch, s);
     return e;
   }
-  pgh::record_kernel("k_split", ga, 256);
   CUtensorMap mA, mB;
   if (!make_map(&mA, al, Kp, LIMBS * nA * g.M, TC_M) ||
       !make_map(&mB, bl, Kp, LIMBS * nB * g.N, TC_N)) {

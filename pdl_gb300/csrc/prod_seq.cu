@@ -49,7 +49,7 @@ template <> struct LogLim<double> {
 // mantissa bits (log2(1 + f) lies in [f, f + 0.0861] for f in [0, 1)).
 template <class Out> __device__ __forceinline__ bool normal_nz(Out x) {
   if constexpr (sizeof(Out) == 8) {
-    const uint32_t e = (uint32_t)((uint64_t)__double_as_longlong(x) >> 52) & 0x7FFu;
+    const uint32_t e = (hi_b32((uint64_t)__double_as_longlong(x)) >> 20) & 0x7FFu;
     return e != 0 && e != 0x7FF;
   } else {
     const uint32_t e = (__float_as_uint(x) >> 23) & 0xFFu;
@@ -58,9 +58,9 @@ template <class Out> __device__ __forceinline__ bool normal_nz(Out x) {
 }
 template <class Out> __device__ __forceinline__ float log2_lo(Out x) {
   if constexpr (sizeof(Out) == 8) {
-    const uint64_t b = (uint64_t)__double_as_longlong(x);
-    const int e = (int)((b >> 52) & 0x7FF) - 1023;
-    const float f = __uint_as_float(0x3F800000u | (uint32_t)((b >> 29) & 0x7FFFFF)) - 1.0f;
+    const uint32_t h = hi_b32((uint64_t)__double_as_longlong(x));
+    const int e = (int)((h >> 20) & 0x7FF) - 1023;
+    const float f = __uint_as_float(0x3F800000u | ((h & 0xFFFFF) << 3)) - 1.0f;
     return (float)e + f;
   } else {
     const uint32_t b = __float_as_uint(x);
@@ -106,7 +106,7 @@ __device__ void suffix_scan(const In *a, int64_t inc, int64_t from, int64_t to, 
     const Out x = (Out)v;
     s.q = mul_rn(s.q, x);
     s.cnt++;
-    if (x == (Out)0) {
+    if (is_zero_bits(x)) {
       if (i < s.z) s.z = i;
     } else if (!normal_nz(x)) {
       s.special = 1;
@@ -156,7 +156,7 @@ __global__ void __launch_bounds__(32) k_prod_seq(const RedArgs args, int64_t S) 
       const In *ar = reinterpret_cast<const In *>(
           __shfl_sync(0xffffffffu, (unsigned long long)a, r));
       const int64_t i = i0 + lane;
-      reg[r] = ((rows_live >> r) & 1u) && i < pend ? ar[i * inc] : (In)0;
+      reg[r] = ((rows_live >> r) & 1u) && i < pend ? ar[i * inc] : (In)1;
     }
   };
   unsigned live_mask = __ballot_sync(0xffffffffu, live);
@@ -169,15 +169,30 @@ __global__ void __launch_bounds__(32) k_prod_seq(const RedArgs args, int64_t S) 
     if (i0 + PS_CH < pend) fetch(i0 + PS_CH, live_mask);
     const int m = (int)(pend - i0 < PS_CH ? pend - i0 : PS_CH);
     if (live) {
+      // the dependent chain is the multiplies alone: a bad element
+      // multiplies by 1, and the first zero product is latched beside the
+      // chain (later products of a zero are never used)
+      Out stop = (Out)0;
+      bool stopped = false;
+#pragma unroll 8
       for (int j = 0; j < m; j++) {
         const In v = tile[j][lane];
-        if (bad_el<In, BAD>(v, bv)) continue;
-        tmp = mul_rn(tmp, (Out)v);
-        cnt++;
-        if (tmp == (Out)0) {
-          live = false;
-          break;
+        Out x = (Out)v;
+        if constexpr (BAD) {
+          const bool b = bad_el<In, BAD>(v, bv);
+          x = b ? (Out)1 : x;
+          cnt += b ? 0 : 1;
+        } else {
+          cnt++;
         }
+        tmp = mul_rn(tmp, x);
+        const bool z = !stopped && is_zero_bits(tmp);
+        stop = z ? tmp : stop;
+        stopped = stopped || z;
+      }
+      if (stopped) {
+        tmp = stop;
+        live = false;
       }
     }
     live_mask = __ballot_sync(0xffffffffu, live);
@@ -221,7 +236,7 @@ __global__ void __launch_bounds__(32) k_prod_seq(const RedArgs args, int64_t S) 
       const In v = a[i * inc];
       if (bad_el<In, BAD>(v, bv)) continue;
       tmp = mul_rn(tmp, (Out)v);
-      if (tmp == (Out)0) break;
+      if (is_zero_bits(tmp)) break;
     }
   }
   if (have) {

@@ -109,7 +109,7 @@ template <class In, class Out, bool COMP> struct OpSum {
 
 // x == 0 on the integer pipe (the float64 compare would use the FP64 pipe)
 template <class T> __device__ __forceinline__ bool is_zero_bits(T x) {
-  if constexpr (sizeof(T) == 8) return ((uint64_t)__double_as_longlong((double)x) << 1) == 0;
+  if constexpr (sizeof(T) == 8) return zero_bits64((uint64_t)__double_as_longlong((double)x));
   else return ((uint32_t)__float_as_uint((float)x) << 1) == 0;
 }
 
@@ -361,8 +361,8 @@ template <class T> struct OpFirstNZ {
 // space (maximum negates the key) NaN is the worst key; equal keys go to
 // the lower index, except NaN against NaN, which goes to the higher index.
 __device__ __forceinline__ int64_t dkey(uint64_t b) {
-  int64_t mag = (int64_t)(b & 0x7FFFFFFFFFFFFFFFull);
-  int64_t s = (int64_t)b >> 63;
+  const int64_t mag = (int64_t)and_b64(b, 0x7FFFFFFFFFFFFFFFull);
+  const int64_t s = (int64_t)b >> 63;
   return (mag ^ s) - s;
 }
 constexpr int64_t KEY_NAN = 0x7FFFFFFFFFFFFFFFll;
@@ -379,7 +379,7 @@ template <bool MAX, bool IND> struct OpMM<double, MAX, IND> {
   __device__ static double neutral() { return 0.0; }
   static constexpr int kU = 8;
   __device__ static int64_t key_of(uint64_t b) {
-    if ((b & 0x7FFFFFFFFFFFFFFFull) > 0x7FF0000000000000ull) return KEY_NAN;
+    if (and_b64(b, 0x7FFFFFFFFFFFFFFFull) > 0x7FF0000000000000ull) return KEY_NAN;
     int64_t k = dkey(b);
     return MAX ? -k : k;
   }
@@ -406,7 +406,7 @@ template <bool MAX, bool IND> struct OpMM<double, MAX, IND> {
     uint32_t special = 0;
 #pragma unroll
     for (int j = 0; j < B; j++) {
-      uint32_t hi = (uint32_t)(bits[j] >> 32);
+      const uint32_t hi = hi_b32(bits[j]);
       special |= (~hi & 0x7FF00000u) == 0;  // exponent all ones: inf or NaN
       int64_t kk = dkey(bits[j]);
       k[j] = MAX ? -kk : kk;
@@ -554,8 +554,17 @@ __device__ __forceinline__ void row_accumulate(const In *row, int64_t lo, int64_
   const int64_t per = (int64_t)G * U;
   int64_t nbad = 0;
   int64_t k = lane;
-  // full iterations: all U vectors in range, no per-vector checks
+  // full iterations: all U vectors in range, no per-vector checks.  The
+  // group's first lane asks L2 for the next iteration's span (G * U
+  // vectors, contiguous, clamped to the row) so HBM stays busy while the
+  // group works on this one.
   for (; k + (int64_t)(U - 1) * G < nv; k += per) {
+    if (lane == 0 && k + per < nv) {
+      const int64_t left = nv - (k + per);
+      const uint32_t bytes = (uint32_t)((left < per ? left : per) * 16);
+      asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(vp + k + per), "r"(bytes)
+                   : "memory");
+    }
     VecT<In, VEC> buf[U];
 #pragma unroll
     for (int u = 0; u < U; u++) buf[u] = ldv(vp + k + (int64_t)u * G);

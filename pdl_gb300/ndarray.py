@@ -735,41 +735,56 @@ def _finish(g: ndarray, use_dev: bool):
     return g
 
 
-def sumover_bwd(gb: ndarray, a: ndarray) -> ndarray:
+def _grads(like, dev, out):
+    """Gradient buffers shaped like `like` (new ones, or the caller's `out`,
+    which must have those dims and type and be on the same side)."""
+    if out is None:
+        return [_grad_like(x, dev) for x in like]
+    out = list(out) if isinstance(out, (tuple, list)) else [out]
+    for o, x in zip(out, like):
+        if o.dims != x.dims or o.datatype != x.datatype:
+            raise PDLError(A.EUSERERROR, f"backward: out has dims {o.dims} type {o.type}, "
+                                         f"needs {x.dims} {x.type}")
+        if dev and not o.on_device:
+            o.to_device()
+    return out
+
+
+def sumover_bwd(gb: ndarray, a: ndarray, out=None) -> ndarray:
     dev = gb.on_device or a.on_device
-    ga = _grad_like(a, dev)
+    (ga,) = _grads([a], dev, out)
     d1, d2 = gb._desc(dev), ga._desc(dev)
     check(lib().pdlgb300_sumover_bwd(C.byref(d1), C.byref(d2)))
     return _finish(ga, dev)
 
 
-def average_bwd(gb: ndarray, a: ndarray) -> ndarray:
+def average_bwd(gb: ndarray, a: ndarray, out=None) -> ndarray:
     dev = gb.on_device or a.on_device
-    ga = _grad_like(a, dev)
+    (ga,) = _grads([a], dev, out)
     d1, d2 = gb._desc(dev), ga._desc(dev)
     check(lib().pdlgb300_average_bwd(C.byref(d1), C.byref(d2)))
     return _finish(ga, dev)
 
 
-def plus_bwd(gc: ndarray, a: ndarray, b: ndarray):
+def plus_bwd(gc: ndarray, a: ndarray, b: ndarray, out=None):
     dev = gc.on_device or a.on_device or b.on_device
-    ga, gb = _grad_like(a, dev), _grad_like(b, dev)
+    ga, gb = _grads([a, b], dev, out)
     d0, d1, d2 = gc._desc(dev), ga._desc(dev), gb._desc(dev)
     check(lib().pdlgb300_plus_bwd(C.byref(d0), C.byref(d1), C.byref(d2)))
     return _finish(ga, dev), _finish(gb, dev)
 
 
-def mult_bwd(gc: ndarray, a: ndarray, b: ndarray):
+def mult_bwd(gc: ndarray, a: ndarray, b: ndarray, out=None):
     dev = gc.on_device or a.on_device or b.on_device
-    ga, gb = _grad_like(a, dev), _grad_like(b, dev)
+    ga, gb = _grads([a, b], dev, out)
     ds = [gc._desc(dev), a._desc(dev), b._desc(dev), ga._desc(dev), gb._desc(dev)]
     check(lib().pdlgb300_mult_bwd(*[C.byref(d) for d in ds]))
     return _finish(ga, dev), _finish(gb, dev)
 
 
-def matmult_bwd(gc: ndarray, a: ndarray, b: ndarray):
+def matmult_bwd(gc: ndarray, a: ndarray, b: ndarray, out=None):
     dev = gc.on_device or a.on_device or b.on_device
-    ga, gb = _grad_like(a, dev), _grad_like(b, dev)
+    ga, gb = _grads([a, b], dev, out)
     ds = [gc._desc(dev), a._desc(dev), b._desc(dev), ga._desc(dev), gb._desc(dev)]
     check(lib().pdlgb300_matmult_bwd(*[C.byref(d) for d in ds]))
     return _finish(ga, dev), _finish(gb, dev)
