@@ -87,15 +87,16 @@ __global__ void __launch_bounds__(FT) k_fused_outer(const FusedArgs g) {
   Bad<T> bt{from_bits<T>(g.tbad), (bool)g.tbad_isnan};
   const T tbad = from_bits<T>(g.tbad), ubad = from_bits<T>(g.ubad);
   typename FA::A acc[4][4];
-  int cnt[4][4];
+  bool cnt[4][4];  // any good pair (sumover's flag), bad-value mode only
 #pragma unroll
   for (int x = 0; x < 4; x++)
 #pragma unroll
     for (int y = 0; y < 4; y++) {
       acc[x][y] = FA::zero();
-      cnt[x][y] = 0;
+      cnt[x][y] = false;
     }
   for (int64_t i0 = 0; i0 < g.n; i0 += FN) {
+    uint32_t gma[4] = {0, 0, 0, 0}, gmb[4] = {0, 0, 0, 0};  // fast path: good bits of the slab
     __syncthreads();
     // stage: FN x FK of a (and d), FN x FJ of b; i fastest across threads
     for (int idx = tid; idx < FN * FK; idx += FT) {
@@ -179,14 +180,29 @@ __global__ void __launch_bounds__(FT) k_fused_outer(const FusedArgs g) {
           fast = false;
         }
         if (fast) {
+          // a pair is counted when its a, d and b are good: kept as bits
+          // of this slab (bit i), tested once per slab
 #pragma unroll
-          for (int y = 0; y < 4; y++)
+          for (int x = 0; x < 4; x++) {
+            gma[x] |= (uint32_t)!ka[x] << i;
+            gmb[x] |= (uint32_t)!xb[x] << i;
+          }
+          if (!(xb[0] || xb[1] || xb[2] || xb[3])) {
+            // no bad b: zeroed a and d make a skipped pair add 0 exactly
 #pragma unroll
-            for (int x = 0; x < 4; x++) {
-              const T u = op_add<T>(op_mul<T>(a0[x], b0[y]), d0[x]);
-              FA::add(acc[y][x], xb[y] ? (T)0 : u);
-              cnt[y][x] += !(ka[x] || xb[y]);
-            }
+            for (int y = 0; y < 4; y++)
+#pragma unroll
+              for (int x = 0; x < 4; x++)
+                FA::add(acc[y][x], op_add<T>(op_mul<T>(a0[x], b0[y]), d0[x]));
+          } else {
+#pragma unroll
+            for (int y = 0; y < 4; y++)
+#pragma unroll
+              for (int x = 0; x < 4; x++) {
+                const T u = op_add<T>(op_mul<T>(a0[x], b0[y]), d0[x]);
+                FA::add(acc[y][x], xb[y] ? (T)0 : u);
+              }
+          }
         } else {
           auto pairs = [&](auto tnan) {
             constexpr bool TN = decltype(tnan)::value;
@@ -199,7 +215,7 @@ __global__ void __launch_bounds__(FT) k_fused_outer(const FusedArgs g) {
                 const T u = ((ft && isbt(t)) || xd[x]) ? ubad : op_add<T>(t, dv[x]);
                 if (!(fu && isbt(u))) {
                   FA::add(acc[y][x], u);
-                  cnt[y][x]++;
+                  cnt[y][x] = true;
                 }
               }
           };
@@ -217,6 +233,12 @@ __global__ void __launch_bounds__(FT) k_fused_outer(const FusedArgs g) {
           }
       }
     }
+    if constexpr (BAD) {
+#pragma unroll
+      for (int y = 0; y < 4; y++)
+#pragma unroll
+        for (int x = 0; x < 4; x++) cnt[y][x] = cnt[y][x] || (gma[x] & gmb[y]) != 0;
+    }
   }
   // write c(j, k): c's inc along the j dim and the k dim
   const int64_t c_j = g.L.inc[3][g.jdim], c_k = g.L.inc[3][g.kdim];
@@ -230,7 +252,7 @@ __global__ void __launch_bounds__(FT) k_fused_outer(const FusedArgs g) {
     for (int x = 0; x < 4; x++) {
       int64_t k = k0 + tk * 4 + x;
       if (k >= K) continue;
-      Out r = (BAD && cnt[y][x] == 0) ? cbad : FA::value(acc[y][x]);
+      Out r = (BAD && !cnt[y][x]) ? cbad : FA::value(acc[y][x]);
       C[j * c_j + k * c_k] = r;
     }
   }

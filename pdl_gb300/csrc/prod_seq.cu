@@ -11,9 +11,9 @@
 //  1. Sequential prefix.  Each warp takes 32 rows, one per lane, and runs
 //     the reference's loop over the first S elements of its row exactly
 //     (same order, one rounding per product, the break).  The warp stages
-//     32 x 32 tiles of its rows through shared memory (coalesced loads,
-//     double-buffered through registers) so the lanes' dependent multiply
-//     chains never wait on scattered loads.  Rows that end or stop inside
+//     64-element chunks of its 32 rows in shared memory with cp.async, two
+//     chunks in flight, so the lanes' dependent multiply chains do not wait
+//     on scattered loads.  Rows that end or stop inside
 //     the prefix are done: uniform[-1,1) data, for one, underflows after
 //     about 750 elements.
 //  2. Suffix check.  For each row that goes on, the warp reads the rest of
@@ -35,7 +35,7 @@
 namespace pg {
 namespace {
 
-constexpr int PS_CH = 32;  // elements per staged chunk of a row
+constexpr int PS_CH = 64;  // elements per staged chunk of a row (a multiple of 32)
 
 template <class Out> struct LogLim;
 template <> struct LogLim<float> {
@@ -130,7 +130,9 @@ __device__ void suffix_scan(const In *a, int64_t inc, int64_t from, int64_t to, 
 
 template <class In, class Out, bool BAD>
 __global__ void __launch_bounds__(32) k_prod_seq(const RedArgs args, int64_t S) {
-  __shared__ In tile[PS_CH][33];  // [element][row]: lane r reads column r
+  // two chunks of PS_CH elements of the warp's 32 rows in flight:
+  // [stage][element][row], a row's elements down one column
+  __shared__ __align__(16) In tile[2][PS_CH][33];
   const int lane = threadIdx.x;
   const int64_t row0 = (int64_t)blockIdx.x * 32;
   const int64_t row = row0 + lane;
@@ -148,25 +150,44 @@ __global__ void __launch_bounds__(32) k_prod_seq(const RedArgs args, int64_t S) 
   int64_t cnt = 0;
   bool live = have;  // still multiplying
   // -------------------------------------------- 1. sequential prefix
-  In reg[PS_CH];
-  auto fetch = [&](int64_t i0, unsigned rows_live) {
-    // lane j loads element i0 + j of every live row of the warp
-#pragma unroll
+  // lane j copies elements i0 + j, i0 + 32 + j, ... of every live row
+  // straight into shared memory (cp.async: nothing held in registers while
+  // in flight); elements past the prefix are zero-filled and never used
+  auto fetch = [&](int st, int64_t i0, unsigned rows_live) {
+#pragma unroll 4
     for (int r = 0; r < 32; r++) {
       const In *ar = reinterpret_cast<const In *>(
           __shfl_sync(0xffffffffu, (unsigned long long)a, r));
-      const int64_t i = i0 + lane;
-      reg[r] = ((rows_live >> r) & 1u) && i < pend ? ar[i * inc] : (In)1;
+#pragma unroll
+      for (int h = 0; h < PS_CH / 32; h++) {
+        const int e = h * 32 + lane;
+        const int64_t i = i0 + e;
+        const bool in = ((rows_live >> r) & 1u) && i < pend;
+        if constexpr (sizeof(In) >= 4) {
+          const uint32_t dst = (uint32_t)__cvta_generic_to_shared(&tile[st][e][r]);
+          const In *src = in ? ar + i * inc : ar;
+          asm volatile("cp.async.ca.shared.global [%0], [%1], %2, %3;" ::"r"(dst), "l"(src),
+                       "n"(sizeof(In)), "r"(in ? (int)sizeof(In) : 0)
+                       : "memory");
+        } else {
+          // (1- and 2-byte types: cp.async copies 4, 8 or 16 bytes)
+          tile[st][e][r] = in ? ar[i * inc] : (In)0;
+        }
+      }
     }
+    asm volatile("cp.async.commit_group;" ::: "memory");
   };
   unsigned live_mask = __ballot_sync(0xffffffffu, live);
-  if (pend > 0 && live_mask) fetch(0, live_mask);
-  for (int64_t i0 = 0; i0 < pend && live_mask; i0 += PS_CH) {
+  if (pend > 0 && live_mask) {
+    fetch(0, 0, live_mask);
+    if (PS_CH < pend) fetch(1, PS_CH, live_mask);
+  }
+  int st = 0;
+  for (int64_t i0 = 0; i0 < pend && live_mask; i0 += PS_CH, st ^= 1) {
+    // this chunk's group has landed (the next one may still be in flight)
+    if (i0 + PS_CH < pend) asm volatile("cp.async.wait_group 1;" ::: "memory");
+    else asm volatile("cp.async.wait_group 0;" ::: "memory");
     __syncwarp();
-#pragma unroll
-    for (int r = 0; r < 32; r++) tile[lane][r] = reg[r];  // element lane of row r
-    __syncwarp();
-    if (i0 + PS_CH < pend) fetch(i0 + PS_CH, live_mask);
     const int m = (int)(pend - i0 < PS_CH ? pend - i0 : PS_CH);
     if (live) {
       // the dependent chain is the multiplies alone: a bad element
@@ -176,7 +197,7 @@ __global__ void __launch_bounds__(32) k_prod_seq(const RedArgs args, int64_t S) 
       bool stopped = false;
 #pragma unroll 8
       for (int j = 0; j < m; j++) {
-        const In v = tile[j][lane];
+        const In v = tile[st][j][lane];
         Out x = (Out)v;
         if constexpr (BAD) {
           const bool b = bad_el<In, BAD>(v, bv);
@@ -196,7 +217,10 @@ __global__ void __launch_bounds__(32) k_prod_seq(const RedArgs args, int64_t S) 
       }
     }
     live_mask = __ballot_sync(0xffffffffu, live);
+    __syncwarp();  // every lane is done with this stage before it is refilled
+    if (i0 + 2 * PS_CH < pend && live_mask) fetch(st, i0 + 2 * PS_CH, live_mask);
   }
+  asm volatile("cp.async.wait_group 0;" ::: "memory");
   // -------------------------------------------- 2. suffix check
   bool seq = false;
   unsigned cont = __ballot_sync(0xffffffffu, live && n > pend);
