@@ -89,9 +89,11 @@ def run(op: str, inputs, outputs=None, swap: int = 0, nthreads: int = 1):
             t = d.datatype
             n = int(np.prod(dims, dtype=np.int64)) if dims else 1
             it = np.dtype(NP_DTYPES[t]).itemsize
-            raw = C.string_at(d.data, n * it) if n else b""
+            # (copied with memmove: string_at's size overflows at 2 GiB)
+            host = np.empty(max(n * it, 1), dtype=np.uint8)
+            if n:
+                C.memmove(host.ctypes.data, d.data, n * it)
             lib().oracle_free(d.data)
-            host = np.frombuffer(bytearray(raw) if raw else bytearray(1), dtype=np.uint8).copy()
             o = ndarray(Storage(n * it, host=host), t, dims)
         o._badflag = bool(d.state & A.BADVAL)
         res.append(o)

@@ -1,0 +1,66 @@
+"""Seeded synthetic inputs of the configurations (the same numpy calls the
+bench makes), shared by the real-PDL fixture script and the tests that
+compare against its fixtures.  numpy's PCG64 streams give the same bytes on
+every platform, and the fixtures record each input's SHA-256 to prove it."""
+import hashlib
+
+import numpy as np
+
+F32_BAD = np.float32(-3.4028234663852886e38)
+
+
+def sha(arr) -> str:
+    return hashlib.sha256(np.ascontiguousarray(arr).tobytes()).hexdigest()
+
+
+def c1():
+    """float64 (4096, 2048) uniform[-1, 1), seed 1 (numpy shape (2048, 4096))."""
+    return {"a": np.random.default_rng(1).uniform(-1.0, 1.0, size=(2048, 4096))}
+
+
+def c5(rows=4096, n=65536, long_n=1 << 27):
+    """float32 (65536, 4096) and one row of 2^27: lognormal(0, 4) magnitudes,
+    random sign, 1 % float's default badvalue, seed 7."""
+    rng = np.random.default_rng(7)
+
+    def gen(count):
+        v = np.exp(np.float32(4.0) * rng.standard_normal(count, dtype=np.float32))
+        v *= np.where(rng.random(count, dtype=np.float32) < 0.5, np.float32(-1), np.float32(1))
+        v[rng.random(count, dtype=np.float32) < 0.01] = F32_BAD
+        return v
+
+    return {"mat": gen(n * rows).reshape(rows, n), "row": gen(long_n).reshape(1, -1)}
+
+
+def c2_int32():
+    """a int32 (256, 1, 8192), b int32 (256, 512, 1), U{-1000..1000}, seed 2."""
+    rng = np.random.default_rng(2)
+    a = rng.integers(-1000, 1001, size=(8192, 1, 256)).astype(np.int32)
+    b = rng.integers(-1000, 1001, size=(1, 512, 256)).astype(np.int32)
+    return {"a": a, "b": b}
+
+
+def c2_float32_bad():
+    """The same shapes, float32 N(0, 1), 2 % of a and of b BAD, seed 3."""
+    rng = np.random.default_rng(3)
+    a = rng.standard_normal((8192, 1, 256)).astype(np.float32)
+    b = rng.standard_normal((1, 512, 256)).astype(np.float32)
+    a[rng.random(a.shape) < 0.02] = F32_BAD
+    b[rng.random(b.shape) < 0.02] = F32_BAD
+    return {"a": a, "b": b}
+
+
+def c3_inner(cols=65536):
+    """float64 a, b (4096, 65536) uniform[-1, 1), seed 5."""
+    rng = np.random.default_rng(5)
+    a = rng.uniform(-1.0, 1.0, size=(cols, 4096))
+    b = rng.uniform(-1.0, 1.0, size=(cols, 4096))
+    return {"a": a, "b": b}
+
+
+def c3_matmult(nb=16):
+    """float32 a(t=1024, h=2048) batch 16, b(w=2048, t=1024), N(0, 1), seed 4."""
+    rng = np.random.default_rng(4)
+    a = rng.standard_normal((nb, 2048, 1024)).astype(np.float32)
+    b = rng.standard_normal((1024, 2048)).astype(np.float32)
+    return {"a": a, "b": b}
