@@ -810,6 +810,8 @@ def main():
                     help="time only the sort-based workload and print its object")
     ap.add_argument("--family-only", action="store_true",
                     help="time only the float64 family (--ops) and print its object")
+    ap.add_argument("--mm-only", action="store_true",
+                    help="time only the float32 matmult workload and print its object")
     ap.add_argument("--c4-only", action="store_true",
                     help="time only the adjoint workload and print its object")
     ap.add_argument("--c2-only", action="store_true",
@@ -825,13 +827,18 @@ def main():
             return 0
         print(json.dumps(run_reference(args, rank, world)))
         return 0
-    if args.expr_only or args.sort_only or args.family_only or args.c2_only or args.c4_only:
+    if (args.expr_only or args.sort_only or args.family_only or args.c2_only or args.c4_only
+            or args.mm_only):
         import torch
         import pdl_gb300 as P
         stream = torch.cuda.current_stream()
         P.set_stream(stream.cuda_stream)
         if args.c2_only or args.c4_only:
             print(json.dumps((bench_c2 if args.c2_only else bench_c4)(args, P, torch, stream)))
+            return 0
+        if args.mm_only:
+            hbm, bf16, kind = peaks()
+            print(json.dumps(bench_matmult(args, P, torch, stream, bf16, kind)))
             return 0
         fn = bench_expr if args.expr_only else bench_sort if args.sort_only else run_family
         print(json.dumps(fn(args, P, torch, stream, peaks()[0])))

@@ -965,12 +965,16 @@ pdlgb300_error dispatch_reduce(RunCtx &c, int redop) {
     lc.block = 128;
     lc.grid = (int)std::min<int64_t>((a.rows + 127) / 128, (int64_t)nsm * 64);
   } else if (a.n * (int64_t)isz <= 32768) {
-    // rows up to 32 KiB: a warp per row, 8 rows per block (a block per row
-    // with 128 bytes per thread measured slower on the float64 (4096, 2048)
-    // family: its 256-thread row merges cost more than the occupancy gained)
+    // rows up to 32 KiB: a warp per row (a block per row with 128 bytes per
+    // thread measured slower on the float64 (4096, 2048) family: its
+    // 256-thread row merges cost more than the occupancy gained).  Up to 8
+    // rows per block, fewer when rows are few, so the blocks spread evenly:
+    // with 2048 rows, 8-row blocks leave the busiest SMs 16 rows against an
+    // average of 13.5; 1-row blocks, 14.
     a.group = 32;
-    lc.block = 256;
-    lc.grid = (int)std::min<int64_t>((a.rows + 7) / 8, (int64_t)1 << 30);
+    const int64_t rpb = std::max<int64_t>(1, std::min<int64_t>(8, a.rows / (8 * (int64_t)nsm)));
+    lc.block = (int)(32 * rpb);
+    lc.grid = (int)std::min<int64_t>((a.rows + rpb - 1) / rpb, (int64_t)1 << 30);
   } else {
     a.group = a.n >= 16384 ? 256 : 128;
     lc.block = a.group;

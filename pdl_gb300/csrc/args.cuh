@@ -36,8 +36,6 @@ struct RedArgs {
   int group;          // threads per row (row kernel)
   int f32_comp;       // compensated float32 sums
   int64_t *zidx;      // floating products: per row, first good exact zero (or INT64_MAX)
-  int async;          // row kernel: contiguous full iterations staged by cp.async
-                      // through the dynamic shared-memory ring (float64 ops)
   int *split_ctr;     // split mode: per-row arrival counters (zero between launches), or
                       // nullptr for a separate combine kernel
 };

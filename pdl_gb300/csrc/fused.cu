@@ -187,22 +187,16 @@ __global__ void __launch_bounds__(FT) k_fused_outer(const FusedArgs g) {
             gma[x] |= (uint32_t)!ka[x] << i;
             gmb[x] |= (uint32_t)!xb[x] << i;
           }
-          if (!(xb[0] || xb[1] || xb[2] || xb[3])) {
-            // no bad b: zeroed a and d make a skipped pair add 0 exactly
+          // (zeroed a and d make a pair with a bad a or d add 0 exactly; a bad
+          // b is selected away; one path for the whole warp: lanes hold 16
+          // different b groups, a branch on them would diverge)
 #pragma unroll
-            for (int y = 0; y < 4; y++)
+          for (int y = 0; y < 4; y++)
 #pragma unroll
-              for (int x = 0; x < 4; x++)
-                FA::add(acc[y][x], op_add<T>(op_mul<T>(a0[x], b0[y]), d0[x]));
-          } else {
-#pragma unroll
-            for (int y = 0; y < 4; y++)
-#pragma unroll
-              for (int x = 0; x < 4; x++) {
-                const T u = op_add<T>(op_mul<T>(a0[x], b0[y]), d0[x]);
-                FA::add(acc[y][x], xb[y] ? (T)0 : u);
-              }
-          }
+            for (int x = 0; x < 4; x++) {
+              const T u = op_add<T>(op_mul<T>(a0[x], b0[y]), d0[x]);
+              FA::add(acc[y][x], xb[y] ? (T)0 : u);
+            }
         } else {
           auto pairs = [&](auto tnan) {
             constexpr bool TN = decltype(tnan)::value;

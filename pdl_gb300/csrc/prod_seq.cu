@@ -190,30 +190,40 @@ __global__ void __launch_bounds__(32) k_prod_seq(const RedArgs args, int64_t S) 
     __syncwarp();
     const int m = (int)(pend - i0 < PS_CH ? pend - i0 : PS_CH);
     if (live) {
-      // the dependent chain is the multiplies alone: a bad element
-      // multiplies by 1, and the first zero product is latched beside the
-      // chain (later products of a zero are never used)
-      Out stop = (Out)0;
-      bool stopped = false;
-#pragma unroll 8
-      for (int j = 0; j < m; j++) {
+      // The chunk's products alone (a bad element multiplies by 1): the
+      // dependent chain is one multiply per element.  A product that reaches
+      // zero stops the reference's loop; later products of a zero are zero
+      // or NaN, so only a chunk that ends zero or NaN is run again from its
+      // start, element by element, to stop at the first zero.
+      const Out start = tmp;
+      auto elem = [&](int j) {
         const In v = tile[st][j][lane];
         Out x = (Out)v;
         if constexpr (BAD) {
           const bool b = bad_el<In, BAD>(v, bv);
           x = b ? (Out)1 : x;
           cnt += b ? 0 : 1;
-        } else {
-          cnt++;
         }
-        tmp = mul_rn(tmp, x);
-        const bool z = !stopped && is_zero_bits(tmp);
-        stop = z ? tmp : stop;
-        stopped = stopped || z;
+        return x;
+      };
+      if (m == PS_CH) {
+#pragma unroll
+        for (int j = 0; j < PS_CH; j++) tmp = mul_rn(tmp, elem(j));
+      } else {
+        for (int j = 0; j < m; j++) tmp = mul_rn(tmp, elem(j));
       }
-      if (stopped) {
-        tmp = stop;
-        live = false;
+      if constexpr (!BAD) cnt += m;
+      if (is_zero_bits(tmp) || tmp != tmp) {
+        tmp = start;
+        for (int j = 0; j < m; j++) {
+          const In v = tile[st][j][lane];
+          if (bad_el<In, BAD>(v, bv)) continue;
+          tmp = mul_rn(tmp, (Out)v);
+          if (is_zero_bits(tmp)) {
+            live = false;
+            break;
+          }
+        }
       }
     }
     live_mask = __ballot_sync(0xffffffffu, live);

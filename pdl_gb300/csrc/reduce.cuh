@@ -526,18 +526,10 @@ template <class V> __device__ __forceinline__ V ldv(const V *p) {
 // Ops with a neutral element (sums, products) add it in place of a bad
 // value, so the inner loop has no branches; the good count is the range
 // size (added by lane 0) minus each lane's bad count.
-// Stages of the cp.async ring of the float64 row kernels (iterations of U
-// vectors per thread; RING_NS - 1 of them in flight beside the one in use).
-constexpr int RING_NS = 3;
-template <class Op, class In> constexpr bool ring_capable() {
-  return sizeof(In) == 8 && Op::kU == 8;
-}
-
 template <class Op, class In, int BM>
 __device__ __forceinline__ void row_accumulate(const In *row, int64_t lo, int64_t hi,
                                                int lane, int G, In bad,
-                                               AccCnt<typename Op::Acc> &ac,
-                                               unsigned char *ring = nullptr) {
+                                               AccCnt<typename Op::Acc> &ac) {
   constexpr int VEC = 16 / sizeof(In);
   constexpr int U = Op::kU ? Op::kU : 16;  // 16-byte vectors in flight per thread
   uint32_t nb = 0;
@@ -562,51 +554,11 @@ __device__ __forceinline__ void row_accumulate(const In *row, int64_t lo, int64_
   const int64_t per = (int64_t)G * U;
   int64_t nbad = 0;
   int64_t k = lane;
-  // full iterations: all U vectors in range, no per-vector checks.  With a
-  // ring, each thread copies its own vectors of the iteration RING_NS - 1
-  // ahead into shared memory ([stage][vector][thread]: conflict-free) and
-  // reads the current one back, so the data in flight holds no registers.
-  const int T = blockDim.x;
-  const uint32_t rbase = ring ? (uint32_t)__cvta_generic_to_shared(ring) : 0u;
-  auto issue = [&](int st, int64_t kk) {
-#pragma unroll
-    for (int u = 0; u < U; u++) {
-      const uint32_t dst = rbase + (uint32_t)(((st * U + u) * T + (int)threadIdx.x) * 16);
-      asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst),
-                   "l"(vp + kk + (int64_t)u * G)
-                   : "memory");
-    }
-  };
-  int stage = 0;
-  if (ring) {
-#pragma unroll
-    for (int s = 0; s < RING_NS - 1; s++) {
-      const int64_t kk = k + (int64_t)s * per;
-      if (kk + (int64_t)(U - 1) * G < nv) issue(s, kk);
-      asm volatile("cp.async.commit_group;" ::: "memory");
-    }
-  }
+  // full iterations: all U vectors in range, no per-vector checks
   for (; k + (int64_t)(U - 1) * G < nv; k += per) {
     VecT<In, VEC> buf[U];
-    if (ring) {
-      const int64_t kn = k + (int64_t)(RING_NS - 1) * per;
-      if (kn + (int64_t)(U - 1) * G < nv) issue((stage + RING_NS - 1) % RING_NS, kn);
-      asm volatile("cp.async.commit_group;" ::: "memory");
-      asm volatile("cp.async.wait_group %0;" ::"n"(RING_NS - 1) : "memory");
 #pragma unroll
-      for (int u = 0; u < U; u++) {
-        const uint32_t src = rbase + (uint32_t)(((stage * U + u) * T + (int)threadIdx.x) * 16);
-        float4 f;
-        asm volatile("ld.shared.v4.f32 {%0,%1,%2,%3}, [%4];"
-                     : "=f"(f.x), "=f"(f.y), "=f"(f.z), "=f"(f.w)
-                     : "r"(src));
-        memcpy(&buf[u], &f, 16);
-      }
-      stage = stage + 1 == RING_NS ? 0 : stage + 1;
-    } else {
-#pragma unroll
-      for (int u = 0; u < U; u++) buf[u] = ldv(vp + k + (int64_t)u * G);
-    }
+    for (int u = 0; u < U; u++) buf[u] = ldv(vp + k + (int64_t)u * G);
     if constexpr (BM == 0 && Op::kBlock) {
       Op::template add_block<VEC, U>(ac.acc, reinterpret_cast<const In *>(buf), i + k * VEC,
                                      (int64_t)G * VEC);
@@ -625,7 +577,6 @@ __device__ __forceinline__ void row_accumulate(const In *row, int64_t lo, int64_
       nbad += nbi;
     }
   }
-  if (ring) asm volatile("cp.async.wait_group 0;" ::: "memory");
   // the last, partial iteration
   if (k < nv) {
 #pragma unroll
@@ -708,18 +659,13 @@ __global__ void __launch_bounds__(512) k_red_rows(const RedArgs args) {
     }
     AC ac{Op::init(), 0};
     if (args.inc_n == 1) {
-      unsigned char *ring = nullptr;
-      if constexpr (ring_capable<Op, In>()) {
-        extern __shared__ __align__(16) unsigned char red_ring[];
-        if (args.async) ring = red_ring;
-      }
       if constexpr (!BAD) {
-        row_accumulate<Op, In, 0>(a, lo, hi, lane, G, bv.val, ac, ring);
+        row_accumulate<Op, In, 0>(a, lo, hi, lane, G, bv.val, ac);
       } else if constexpr (std::is_floating_point_v<In>) {
-        if (bv.isnan_) row_accumulate<Op, In, 2>(a, lo, hi, lane, G, bv.val, ac, ring);
-        else row_accumulate<Op, In, 1>(a, lo, hi, lane, G, bv.val, ac, ring);
+        if (bv.isnan_) row_accumulate<Op, In, 2>(a, lo, hi, lane, G, bv.val, ac);
+        else row_accumulate<Op, In, 1>(a, lo, hi, lane, G, bv.val, ac);
       } else {
-        row_accumulate<Op, In, 1>(a, lo, hi, lane, G, bv.val, ac, ring);
+        row_accumulate<Op, In, 1>(a, lo, hi, lane, G, bv.val, ac);
       }
     } else
       row_accumulate_strided<Op, In, BAD>(a, args.inc_n, lo, hi, lane, G, bv, ac);
@@ -879,27 +825,8 @@ pdlgb300_error launch_red_typed(RedArgs args, const RedLaunch &lc, cudaStream_t 
     launched("k_red_thread", lc.grid, lc.block);
     return e;
   }
-  size_t ring = 0;
-  if constexpr (ring_capable<Op, In>()) {
-    // float64 rows: a cp.async ring of RING_NS iterations per thread
-    if (args.inc_n == 1 && lc.block <= 256) {
-      ring = (size_t)RING_NS * Op::kU * lc.block * 16;
-      constexpr int most = RING_NS * Op::kU * 256 * 16;  // the largest block's ring
-      static bool set[2] = {false, false};
-      if (!set[args.bad ? 1 : 0]) {
-        cudaError_t ce =
-            args.bad ? cudaFuncSetAttribute(k_red_rows<Op, In, Out, true>,
-                                            cudaFuncAttributeMaxDynamicSharedMemorySize, most)
-                     : cudaFuncSetAttribute(k_red_rows<Op, In, Out, false>,
-                                            cudaFuncAttributeMaxDynamicSharedMemorySize, most);
-        if (!pgh::cuda_check(ce, &e, "k_red_rows shared memory")) return e;
-        set[args.bad ? 1 : 0] = true;
-      }
-      args.async = 1;
-    }
-  }
-  if (args.bad) k_red_rows<Op, In, Out, true><<<lc.grid, lc.block, ring, s>>>(args);
-  else k_red_rows<Op, In, Out, false><<<lc.grid, lc.block, ring, s>>>(args);
+  if (args.bad) k_red_rows<Op, In, Out, true><<<lc.grid, lc.block, 0, s>>>(args);
+  else k_red_rows<Op, In, Out, false><<<lc.grid, lc.block, 0, s>>>(args);
   if (!launched("k_red_rows", lc.grid, lc.block)) return e;
   if (args.nsplit > 1 && !args.split_ctr) {
     const int g = (int)std::min<int64_t>((args.rows + 3) / 4, 65535);
@@ -922,11 +849,8 @@ template <class Op> size_t acc_size() { return sizeof(typename Op::Acc); }
 template <class Op, class In, class Out>
 int red_occ_typed(bool bad, int block) {
   int occ = 0;
-  size_t ring = 0;
-  if constexpr (ring_capable<Op, In>())
-    if (block <= 256) ring = (size_t)RING_NS * Op::kU * block * 16;
-  if (bad) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_red_rows<Op, In, Out, true>, block, ring);
-  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_red_rows<Op, In, Out, false>, block, ring);
+  if (bad) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_red_rows<Op, In, Out, true>, block, 0);
+  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_red_rows<Op, In, Out, false>, block, 0);
   return occ > 0 ? occ : 1;
 }
 
