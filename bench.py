@@ -40,6 +40,7 @@ import numpy as np
 
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
+sys.path.insert(1, str(ROOT / "tests"))  # config_inputs: the configurations' seeded inputs
 
 UFUNC_OPS = ["sumover", "prodover", "average", "minimum", "maximum", "minimum_ind",
              "cumusumover"]
@@ -72,19 +73,11 @@ def c1_input():
 
 def c5_inputs(rows=None, long_row=True):
     """float32 (rows, n) matrix and one long row: lognormal(0, 4) magnitude,
-    random sign, 1% set to float's default badvalue (-FLT_MAX)."""
-    rows = rows or C5_ROWS
-    rng = np.random.default_rng(7)
-    bad = np.float32(-3.4028234663852886e38)
-
-    def gen(count):
-        v = np.exp(np.float32(4.0) * rng.standard_normal(count, dtype=np.float32))
-        v *= np.where(rng.random(count, dtype=np.float32) < 0.5, np.float32(-1), np.float32(1))
-        v[rng.random(count, dtype=np.float32) < 0.01] = bad
-        return v
-
-    mat = gen(C5_N * rows).reshape(rows, C5_N)
-    return mat, (gen(C5_LONG) if long_row else None)
+    random sign, 1% set to float's default badvalue (-FLT_MAX); the seeded
+    generator shared with the tests (the same bits on every platform)."""
+    import config_inputs as CI
+    d = CI.c5(rows=rows or C5_ROWS, long_n=C5_LONG if long_row else 0)
+    return d["mat"], (d["row"].reshape(-1) if long_row else None)
 
 
 def op_bytes(op, n=N0, rows=N1, isz=8, osz=8):

@@ -18,18 +18,43 @@ def c1():
     return {"a": np.random.default_rng(1).uniform(-1.0, 1.0, size=(2048, 4096))}
 
 
+def exp_portable(x: np.ndarray) -> np.ndarray:
+    """exp(x) for float32 x with the same bits on every platform (numpy's
+    vectorised exp differs between x86 and Arm in the last bits): only IEEE
+    float32 multiplies, adds, floor and ldexp.  x = (e + f) ln 2 with e an
+    integer and f in [0, 1); 2^f from its degree-9 Taylor series (relative
+    error below 1e-6, ample for drawing lognormal magnitudes)."""
+    x = np.asarray(x, dtype=np.float32)
+    t = x * np.float32(1.4426950408889634)
+    e = np.floor(t)
+    g = (t - e) * np.float32(0.6931471805599453)
+    p = np.ones_like(g)
+    for k in range(9, 0, -1):
+        p *= g
+        p *= np.float32(1.0 / k)
+        p += np.float32(1.0)
+    return np.ldexp(p, e.astype(np.int32))
+
+
 def c5(rows=4096, n=65536, long_n=1 << 27):
-    """float32 (65536, 4096) and one row of 2^27: lognormal(0, 4) magnitudes,
-    random sign, 1 % float's default badvalue, seed 7."""
+    """float32 (65536, 4096) and one row of 2^27: lognormal(0, 4) magnitudes
+    (exp(4 z), z standard normal), random sign, 1 % float's default badvalue,
+    seed 7."""
     rng = np.random.default_rng(7)
 
     def gen(count):
-        v = np.exp(np.float32(4.0) * rng.standard_normal(count, dtype=np.float32))
-        v *= np.where(rng.random(count, dtype=np.float32) < 0.5, np.float32(-1), np.float32(1))
-        v[rng.random(count, dtype=np.float32) < 0.01] = F32_BAD
-        return v
+        out = np.empty(count, dtype=np.float32)
+        step = 1 << 24
+        for s in range(0, count, step):                 # bounded temporaries
+            m = min(step, count - s)
+            z = rng.standard_normal(m, dtype=np.float32)
+            out[s:s + m] = exp_portable(np.float32(4.0) * z)
+        out *= np.where(rng.random(count, dtype=np.float32) < 0.5, np.float32(-1), np.float32(1))
+        out[rng.random(count, dtype=np.float32) < 0.01] = F32_BAD
+        return out
 
-    return {"mat": gen(n * rows).reshape(rows, n), "row": gen(long_n).reshape(1, -1)}
+    mat = gen(n * rows).reshape(rows, n)
+    return {"mat": mat, "row": gen(long_n).reshape(1, -1) if long_n else None}
 
 
 def c2_int32():

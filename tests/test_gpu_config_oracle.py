@@ -71,16 +71,10 @@ def test_c1_family_against_the_oracle(gpu, c1, op):
 
 # --------------------------------- float32 (65536, 4096) + 2^27 row, 1 % BAD
 
-def _c5(rows=4096, n=65536, long_n=1 << 27):
-    rng = np.random.default_rng(7)
-
-    def gen(count):
-        v = np.exp(np.float32(4.0) * rng.standard_normal(count, dtype=np.float32))
-        v *= np.where(rng.random(count, dtype=np.float32) < 0.5, np.float32(-1), np.float32(1))
-        v[rng.random(count, dtype=np.float32) < 0.01] = F32_BAD
-        return v
-
-    return gen(n * rows).reshape(rows, n), gen(long_n).reshape(1, -1)
+def _c5():
+    import config_inputs as CI
+    d = CI.c5()
+    return d["mat"], d["row"]
 
 
 @pytest.fixture(scope="module")

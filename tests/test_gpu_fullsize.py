@@ -28,16 +28,10 @@ F32_BAD = np.float32(-3.4028234663852886e38)
 EPS32, EPS64 = 2.0 ** -24, 2.0 ** -53
 
 
-def _c5_inputs(rows=4096, n=65536, long_n=1 << 27):
-    rng = np.random.default_rng(7)
-
-    def gen(count):
-        v = np.exp(np.float32(4.0) * rng.standard_normal(count, dtype=np.float32))
-        v *= np.where(rng.random(count, dtype=np.float32) < 0.5, np.float32(-1), np.float32(1))
-        v[rng.random(count, dtype=np.float32) < 0.01] = F32_BAD
-        return v
-
-    return gen(n * rows).reshape(rows, n), gen(long_n)
+def _c5_inputs():
+    import config_inputs as CI
+    d = CI.c5()
+    return d["mat"], d["row"].reshape(-1)
 
 
 @pytest.fixture(scope="module")
