@@ -124,6 +124,12 @@ typedef struct pdlgb300_vtable {
  * Returns NULL for an unknown name. */
 const pdlgb300_vtable *pdlgb300_get_vtable(const char *name);
 
+/* The Perl package that defines an op ("PDL::Ufunc::", "PDL::Ops::",
+ * "PDL::Primitive::"; "" for an op PDL does not have): PDL names an op in
+ * its error messages by the package-qualified pp_def name
+ * (lib/PDL/PP.pm vtable names), so a caller forming PDL's text prefixes it. */
+const char *pdlgb300_op_package(const char *name);
+
 /* Host-only shaping: the type selection, dim checks and output creation of
  * pdl_type_coerce + pdl_redodims_default (lib/PDL/Core/pdlapi.c:829-869,
  * 1169-1327; lib/PDL/Core/pdlbroadcast.c:211-523).  Null outputs get their

@@ -218,6 +218,19 @@ static int set_err(errbuf *e, const char *fmt, ...) {
 }
 
 /* pdl_param_error, lib/PDL/Core/pdlutil.c:65-147 */
+/* The package defining an op: pdl_param_error uses the package-qualified
+ * vtable name ("PDL::Ops::plus"; PDL's pp_def vtables). */
+static const char *op_package(const char *name) {
+  static const char *const ops[] = {"plus", "mult", "minus", "divide", "gt", "lt", "le", "ge",
+                                    "eq", "ne", "shiftleft", "shiftright", "or2", "and2", "xor"};
+  for (size_t k = 0; k < sizeof ops / sizeof ops[0]; k++)
+    if (!strcmp(name, ops[k])) return "PDL::Ops::";
+  if (!strcmp(name, "inner") || !strcmp(name, "matmult")) return "PDL::Primitive::";
+  return "PDL::Ufunc::";
+}
+
+const char *oracle_op_package(const char *name) { return op_package(name); }
+
 static int param_error(errbuf *e, const opdef *op, int param,
                        pdlgb300_ndarray *const *pdls, int64_t nimpl,
                        const int *creating, const char *fmt, ...) {
@@ -228,7 +241,7 @@ static int param_error(errbuf *e, const opdef *op, int param,
   if (param < 0 || param >= op->npdls) {
     snprintf(msg, sizeof msg, "ERROR: UNKNOWN PARAMETER");
   } else {
-    snprintf(msg, sizeof msg, "%s(", op->name);
+    snprintf(msg, sizeof msg, "%s%s(", op_package(op->name), op->name);
     for (int i = 0; i < op->npdls; i++) {
       ADV();
       snprintf(msg + off, sizeof msg - off, "%s%s", op->par_names[i],
@@ -365,7 +378,8 @@ static int do_redodims(errbuf *e, const opdef *op, pdlgb300_ndarray *const *pdls
   for (int j = 0; j < np; j++) {
     creating[j] = (j >= op->nparents) && (pdls[j]->state & PDLGB300_NOMYDIMS);
     if (j < op->nparents && (pdls[j]->state & PDLGB300_NOMYDIMS))
-      return set_err(e, "%s: input parameter %s is null", op->name, op->par_names[j]);
+      return set_err(e, "Error in %s%s: input parameter '%s' is null", op_package(op->name),
+                     op->name, op->par_names[j]);
     if (creating[j]) continue;
     int64_t k = pdls[j]->ndims - op->realdims[j];
     if (k > nimpl) nimpl = k;
@@ -1393,6 +1407,12 @@ int oracle_npdls(const char *opname) {
   return op < 0 ? -1 : OPS[op].npdls;
 }
 
+/* Name of an op's parameter j (the pp_def signature's), or NULL. */
+const char *oracle_par_name(const char *opname, int j) {
+  int op = find_op(opname);
+  return op < 0 || j < 0 || j >= OPS[op].npdls ? NULL : OPS[op].par_names[j];
+}
+
 int oracle_run(const char *opname, pdlgb300_ndarray **pdls_in, const int64_t *other,
                int nthreads, char *msg, size_t msglen) {
   errbuf e = {msg, msglen};
@@ -1435,10 +1455,6 @@ int oracle_run(const char *opname, pdlgb300_ndarray **pdls_in, const int64_t *ot
       p->state &= ~PDLGB300_NOMYDIMS;
       *pdls_in[j] = *p; /* the caller gets the shape and data back */
     } else if (p->datatype != want) {
-      if (j >= d->nparents)
-        return set_err(&e, "%s: output %s has type %s, needs %s", d->name,
-                       d->par_names[j], oracle_type_name(p->datatype),
-                       oracle_type_name(want));
       /* pdl_get_convertedpdl (pdlapi.c:141-165) makes a converttypei child:
        * its CHILD parameter is PDL_PARAM_ISIGNORE, so the child keeps
        * has_badvalue = 0 (pdlapi.c:1240-1258) and its badvalue is the new
@@ -1509,6 +1525,32 @@ int oracle_run(const char *opname, pdlgb300_ndarray **pdls_in, const int64_t *ot
   /* badflag propagation (pdlapi.c:806-808) and PDLSTATESETBAD */
   for (int j = d->nparents; j < d->npdls; j++) {
     if (bvalflag || c.setbad_out) pdls_in[j]->state |= PDLGB300_BADVAL;
+  }
+  /* A supplied output of another type got a converted child above; its
+   * values flow back into the output (converttypei's writeback, pdlconv.c
+   * COPYCONVERT), a bad value becoming the output's badvalue. */
+  for (int j = d->nparents; j < d->npdls; j++) {
+    if (!tofree[j]) continue;
+    const pdlgb300_ndarray *u = pdls_in[j], *w = pdls[j];
+    int64_t n = 1;
+    for (int i = 0; i < u->ndims; i++) n *= u->dims[i];
+    const size_t ws = type_size(w->datatype), us = type_size(u->datatype);
+    const pdlgb300_value wb = badval_of(w), ub = badval_of(u);
+    int64_t idx[PDLGB300_MAXDIMS] = {0};
+    for (int64_t k = 0; k < n; k++) {
+      int64_t off = u->offs;
+      for (int i = 0; i < u->ndims; i++) off += idx[i] * u->incs[i];
+      char *dst = (char *)u->data + off * (int64_t)us;
+      const char *src = (const char *)w->data + k * (int64_t)ws;
+      if (bvalflag && value_isbad(w->datatype, src, wb))
+        store_value(u->datatype, dst, ub);
+      else
+        convert_elem(w->datatype, src, u->datatype, dst);
+      for (int i = 0; i < u->ndims; i++) {
+        if (++idx[i] < u->dims[i]) break;
+        idx[i] = 0;
+      }
+    }
   }
   for (int j = 0; j < d->npdls; j++) free(tofree[j]);
   return 0;

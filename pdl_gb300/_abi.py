@@ -81,6 +81,7 @@ SIGNATURES = {
     "pdlgb300_get_default_badvalue": (Error, [C.c_int32, C.POINTER(Anyval)]),
     "pdlgb300_set_default_badvalue": (Error, [C.c_int32, Anyval]),
     "pdlgb300_get_vtable": (C.POINTER(Vtable), [C.c_char_p]),
+    "pdlgb300_op_package": (C.c_char_p, [C.c_char_p]),
     "pdlgb300_redodims": (Error, [C.POINTER(Vtable), PP, C.POINTER(C.c_int64)]),
     "pdlgb300_run": (Error, [C.POINTER(Vtable), PP, C.POINTER(C.c_int64)]),
     "pdlgb300_run_sumover": (Error, [P, P]),

@@ -265,8 +265,21 @@ void default_incs(pdlgb300_ndarray *x) {
   }
 }
 
-// pdl_param_error's message: "op(a,b,c): parameter 'b': <msg>" followed by
-// the table of active and broadcast dims.
+// The package that defines an op: pdl_param_error names the op by its
+// vtable name, which is package-qualified ("PDL::Ops::plus").
+const char *op_package(const char *name) {
+  static const char *const ops[] = {"plus", "mult", "minus", "divide", "gt", "lt", "le", "ge",
+                                    "eq", "ne", "shiftleft", "shiftright", "or2", "and2",
+                                    "xor"};
+  for (const char *o : ops)
+    if (!strcmp(name, o)) return "PDL::Ops::";
+  if (!strcmp(name, "inner") || !strcmp(name, "matmult")) return "PDL::Primitive::";
+  if (!strcmp(name, "sumover_mult_plus")) return "";  // no PDL counterpart
+  return "PDL::Ufunc::";
+}
+
+// pdl_param_error's message: "PDL::Pkg::op(a,b,c): parameter 'b': <msg>"
+// followed by the table of active and broadcast dims.
 pdlgb300_error param_error(const pdlgb300_vtable *vt, int param, pdlgb300_ndarray *const *pdls,
                            int nimpl, const int *creating, const char *fmt, ...) {
   std::string m;
@@ -274,7 +287,7 @@ pdlgb300_error param_error(const pdlgb300_vtable *vt, int param, pdlgb300_ndarra
   if (param < 0 || param >= vt->npdls) {
     m = "ERROR: UNKNOWN PARAMETER";
   } else {
-    m = std::string(vt->name) + "(";
+    m = std::string(op_package(vt->name)) + vt->name + "(";
     for (int i = 0; i < vt->npdls; i++) {
       m += vt->par_names[i];
       if (i < vt->npdls - 1) m += ",";
@@ -340,8 +353,8 @@ pdlgb300_error plan_broadcast(const pdlgb300_vtable *vt, pdlgb300_ndarray *const
   for (int j = 0; j < np; j++) {
     b.creating[j] = j >= vt->nparents && (pdls[j]->state & PDLGB300_NOMYDIMS);
     if (j < vt->nparents && (pdls[j]->state & PDLGB300_NOMYDIMS))
-      return err(PDLGB300_EUSERERROR, "%s: input parameter '%s' is null", vt->name,
-                 vt->par_names[j]);
+      return err(PDLGB300_EUSERERROR, "Error in %s%s: input parameter '%s' is null",
+                 op_package(vt->name), vt->name, vt->par_names[j]);
     if (b.creating[j]) continue;
     if (pdls[j]->ndims < 0 || pdls[j]->ndims > PDLGB300_MAXDIMS)
       return err(PDLGB300_EUSERERROR, "%s: parameter '%s' has %d dims (max %d)", vt->name,
@@ -2060,6 +2073,8 @@ pdlgb300_error pdlgb300_sync(void) {
   }
   return ok();
 }
+const char *pdlgb300_op_package(const char *name) { return name ? op_package(name) : ""; }
+
 pdlgb300_error pdlgb300_device_count(int32_t *n) {
   int c = 0;
   cudaError_t e = cudaGetDeviceCount(&c);

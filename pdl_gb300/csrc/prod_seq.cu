@@ -28,10 +28,8 @@
 //  3. Sequential continuation.  Rows whose products may leave the normal
 //     range run the reference's loop on from the prefix, one lane each.
 //
-// The sequential float64 chain multiplies on the integer pipe (dmul_rn_int,
-// bit-identical to the hardware multiply): the chain is latency-bound and
-// GB300's FP64 multiply has the longer latency; the warp-wide suffix
-// products, throughput-bound, stay on the FP64 pipe.
+// The float64 products use the FP64 pipe (__dmul_rn): the dependent chain
+// is latency-bound and the hardware multiply has the shortest latency.
 #include "reduce.cuh"
 
 namespace pg {
@@ -75,13 +73,6 @@ constexpr float LOG2_SLACK = 0.0861f;
 
 template <class Out> __device__ __forceinline__ Out mul_rn(Out a, Out b) {
   if constexpr (sizeof(Out) == 8) return __dmul_rn(a, b);
-  else return __fmul_rn(a, b);
-}
-// The sequential chain's multiply: for float64 the integer-pipe product
-// (dmul_rn_int, the same bits as __dmul_rn) -- GB300's FP64 multiply has a
-// long latency, and on a dependent chain latency is all that counts.
-template <class Out> __device__ __forceinline__ Out mul_chain(Out a, Out b) {
-  if constexpr (sizeof(Out) == 8) return dmul_rn_int(a, b);
   else return __fmul_rn(a, b);
 }
 
@@ -217,9 +208,9 @@ __global__ void __launch_bounds__(32) k_prod_seq(const RedArgs args, int64_t S) 
       };
       if (m == PS_CH) {
 #pragma unroll
-        for (int j = 0; j < PS_CH; j++) tmp = mul_chain(tmp, elem(j));
+        for (int j = 0; j < PS_CH; j++) tmp = mul_rn(tmp, elem(j));
       } else {
-        for (int j = 0; j < m; j++) tmp = mul_chain(tmp, elem(j));
+        for (int j = 0; j < m; j++) tmp = mul_rn(tmp, elem(j));
       }
       if constexpr (!BAD) cnt += m;
       if (is_zero_bits(tmp) || tmp != tmp) {

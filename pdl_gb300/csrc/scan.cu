@@ -557,183 +557,6 @@ __global__ void __launch_bounds__(chain_threads<In, Out>(), (sizeof(In) == 4 && 
   }
 }
 
-// Warp-granular chained scan (equal-width 4- and 8-byte types): each warp
-// is a chain unit of 32 threads x 128 bytes.  A warp loads its unit into its own
-// swizzled shared-memory tile, scans its thread totals, publishes the unit's
-// aggregate, looks back over its predecessors itself (the same decoupled
-// look-back as k_scan_chain, 32 slots per round) and writes its outputs:
-// no block barrier anywhere, so no warp waits while another looks back.
-constexpr int WC_WARPS = 16;  // warps per block (independent units)
-
-template <class In, class Out> constexpr bool wchain_ok() {
-  return sizeof(In) == sizeof(Out) && (sizeof(In) == 4 || sizeof(In) == 8);
-}
-
-template <class In, class Out, int BM, int COMP>
-__global__ void __launch_bounds__(WC_WARPS * 32, 3) k_scan_wchain(const ScanArgs g, int64_t u0) {
-  using S = ScanT<In, Out, COMP>;
-  using Acc = typename S::Acc;
-  constexpr int ITEMS = 128 / sizeof(In);  // 32 per thread
-  constexpr int VEC = 16 / sizeof(In);
-  constexpr int NV = ITEMS / VEC;           // 8 vectors per thread
-  constexpr int WSPAN = 32 * ITEMS;         // elements per unit
-  constexpr int WIN_B = 32 * NV * 16;       // tile bytes per warp
-  extern __shared__ __align__(16) unsigned char sm_tile[];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int64_t u = u0 + (int64_t)blockIdx.x * WC_WARPS + warp;
-  if (u >= g.rows * (int64_t)g.nchunk) return;  // (a whole warp: no barrier follows)
-  const uint32_t sin = (uint32_t)__cvta_generic_to_shared(sm_tile) + (uint32_t)(warp * WIN_B);
-  const int64_t row = u / g.nchunk;
-  const int c = (int)(u - row * g.nchunk);
-  int64_t offs[MAXP];
-  loop_offsets(g.L, row, offs);
-  const In *a = reinterpret_cast<const In *>(g.a) + offs[0];
-  const int64_t wlo = (int64_t)c * WSPAN;
-  const int64_t hi = wlo + WSPAN < g.n ? wlo + WSPAN : g.n;
-  const bool fast = wlo + WSPAN <= hi;
-  const In bad = from_bits<In>(g.abad);
-  auto slot = [&](int q) { return sin + (uint32_t)(lane * NV * 16 + ((q ^ (lane & 7)) * 16)); };
-  auto ldin = [&](int q, In (&x)[VEC]) {
-    float4 f;
-    asm volatile("ld.shared.v4.f32 {%0,%1,%2,%3}, [%4];"
-                 : "=f"(f.x), "=f"(f.y), "=f"(f.z), "=f"(f.w)
-                 : "r"(slot(q)));
-    memcpy(x, &f, 16);
-  };
-  int nvalid = ITEMS;
-  const int64_t t0 = wlo + (int64_t)lane * ITEMS;
-  if (fast) {
-#pragma unroll
-    for (int r = 0; r < NV; r++) {
-      const int gv = r * 32 + lane;
-      const int own = gv / NV, q = gv % NV;
-      const uint32_t dst = sin + (uint32_t)(own * NV * 16 + ((q ^ (own & 7)) * 16));
-      asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst),
-                   "l"(a + wlo + (int64_t)gv * VEC)
-                   : "memory");
-    }
-    asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;" ::: "memory");
-    __syncwarp();
-  } else {
-    const int64_t left = hi - t0;
-    nvalid = left <= 0 ? 0 : (left >= ITEMS ? ITEMS : (int)left);
-#pragma unroll
-    for (int q = 0; q < NV; q++) {
-      In x[VEC];
-#pragma unroll
-      for (int e = 0; e < VEC; e++) x[e] = q * VEC + e < nvalid ? a[t0 + q * VEC + e] : S::pad();
-      float4 f;
-      memcpy(&f, x, 16);
-      asm volatile("st.shared.v4.f32 [%0], {%1,%2,%3,%4};" ::"r"(slot(q)), "f"(f.x), "f"(f.y),
-                   "f"(f.z), "f"(f.w)
-                   : "memory");
-    }
-  }
-  auto good = [&](In x) { return !is_bad<In, BM>(x, bad); };
-  Acc tot = S::zero();
-  if constexpr (std::is_same_v<In, double> && std::is_same_v<Out, double> && !S::kProd) {
-    // float64: two exact 8-element blocks (integer alignment, one FP64 add each)
-    F64Sum fs{0.0};
-#pragma unroll
-    for (int h = 0; h < 2; h++) {
-      double w[NV];
-#pragma unroll
-      for (int q = 0; q < NV / 2; q++) {
-        In x[VEC];
-        ldin(h * (NV / 2) + q, x);
-#pragma unroll
-        for (int e = 0; e < VEC; e++) w[q * VEC + e] = good(x[e]) ? x[e] : 0.0;
-      }
-      fs.add_block<NV>(w);
-    }
-    tot = fs.s;
-  } else {
-#pragma unroll
-    for (int q = 0; q < NV; q++) {
-      In x[VEC];
-      ldin(q, x);
-#pragma unroll
-      for (int e = 0; e < VEC; e++)
-        if (good(x[e])) tot = S::add1(tot, x[e]);
-    }
-  }
-  Acc inc = tot;
-#pragma unroll
-  for (int d = 1; d < 32; d <<= 1) {
-    Acc o = shfl_up_any(inc, d);
-    if (lane >= d) inc = S::add(o, inc);
-  }
-  Acc lex = shfl_up_any(inc, 1);
-  if (lane == 0) lex = S::zero();
-  const Acc agg = shfl_any(inc, 31);
-  Acc excl = S::zero();
-  if (g.nchunk > 1) {
-    ChainSlot *slots = reinterpret_cast<ChainSlot *>(g.status);
-    const uint64_t gid = g.gid_base + (uint64_t)u;
-    if (c == 0) {
-      if (lane == 0) chain_publish(&slots[gid & g.status_mask], gid, 2, acc_to_u64(agg));
-    } else {
-      if (lane == 0) chain_publish(&slots[gid & g.status_mask], gid, 1, acc_to_u64(agg));
-      excl = chain_lookback<S, Acc>(g, slots, gid, c, lane);
-      if (lane == 0)
-        chain_publish(&slots[gid & g.status_mask], gid, 2, acc_to_u64(S::add(excl, agg)));
-    }
-  }
-  Acc run = S::add(excl, lex);
-  const Out obad = from_bits<Out>(g.bbad);
-#pragma unroll
-  for (int q = 0; q < NV; q++) {
-    In x[VEC];
-    ldin(q, x);
-    Out o[VEC];
-#pragma unroll
-    for (int e = 0; e < VEC; e++) {
-      if (good(x[e])) {
-        run = S::add1(run, x[e]);
-        o[e] = S::value(run);
-      } else {
-        o[e] = obad;
-      }
-    }
-    float4 f;
-    memcpy(&f, o, 16);
-    asm volatile("st.shared.v4.f32 [%0], {%1,%2,%3,%4};" ::"r"(slot(q)), "f"(f.x), "f"(f.y),
-                 "f"(f.z), "f"(f.w)
-                 : "memory");
-  }
-  __syncwarp();
-  Out *b = reinterpret_cast<Out *>(g.b) + offs[1];
-  if (fast) {
-#pragma unroll
-    for (int r = 0; r < NV; r++) {
-      const int gv = r * 32 + lane;
-      const int own = gv / NV, q = gv % NV;
-      const uint32_t src = sin + (uint32_t)(own * NV * 16 + ((q ^ (own & 7)) * 16));
-      float4 f;
-      asm volatile("ld.shared.v4.f32 {%0,%1,%2,%3}, [%4];"
-                   : "=f"(f.x), "=f"(f.y), "=f"(f.z), "=f"(f.w)
-                   : "r"(src));
-      __stcs(reinterpret_cast<float4 *>(b + wlo + (int64_t)gv * VEC), f);
-    }
-  } else {
-    for (int j = 0; j < nvalid; j++) {
-      const int q = j / VEC;
-      const uint32_t src = slot(q) + (uint32_t)((j % VEC) * sizeof(Out));
-      Out o;
-      if constexpr (sizeof(Out) == 8) {
-        unsigned long long w;
-        asm volatile("ld.shared.u64 %0, [%1];" : "=l"(w) : "r"(src));
-        memcpy(&o, &w, 8);
-      } else {
-        unsigned int w;
-        asm volatile("ld.shared.u32 %0, [%1];" : "=r"(w) : "r"(src));
-        memcpy(&o, &w, 4);
-      }
-      b[t0 + j] = o;
-    }
-  }
-}
-
 // One thread per row, any increments, the reference's order.
 template <class In, class Out, bool BAD, int COMP>
 __global__ void k_scan_thread(const ScanArgs g) {
@@ -767,30 +590,7 @@ template <class In, class Out> constexpr bool chain_ok() {
 template <class In, class Out, int COMP>
 pdlgb300_error scan_chain_typed(ScanArgs g, cudaStream_t s) {
   pdlgb300_error e = pgh::ok();
-  if constexpr (wchain_ok<In, Out>()) {
-    constexpr size_t smem = (size_t)WC_WARPS * 32 * 128;
-    static bool attr = false;
-    if (!attr) {
-      cudaFuncSetAttribute(k_scan_wchain<In, Out, 0, COMP>,
-                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      cudaFuncSetAttribute(k_scan_wchain<In, Out, 1, COMP>,
-                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      cudaFuncSetAttribute(k_scan_wchain<In, Out, 2, COMP>,
-                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      attr = true;
-    }
-    const int64_t units = g.rows * g.nchunk;
-    const int64_t per = ((int64_t)1 << 30) * WC_WARPS;
-    for (int64_t u0 = 0; u0 < units; u0 += per) {
-      const int64_t nu = std::min<int64_t>(units - u0, per);
-      const int grid = (int)((nu + WC_WARPS - 1) / WC_WARPS);
-      if (!g.bad) k_scan_wchain<In, Out, 0, COMP><<<grid, WC_WARPS * 32, smem, s>>>(g, u0);
-      else if (g.abad_isnan) k_scan_wchain<In, Out, 2, COMP><<<grid, WC_WARPS * 32, smem, s>>>(g, u0);
-      else k_scan_wchain<In, Out, 1, COMP><<<grid, WC_WARPS * 32, smem, s>>>(g, u0);
-      if (!pgh::cuda_check(cudaGetLastError(), &e, "k_scan_wchain")) return e;
-      pgh::record_kernel("k_scan_wchain", grid, WC_WARPS * 32);
-    }
-  } else if constexpr (chain_ok<In, Out>()) {
+  if constexpr (chain_ok<In, Out>()) {
     constexpr int ITEMS = 128 / sizeof(In);
     constexpr int CB = chain_threads<In, Out>();
     constexpr size_t smem = (size_t)CB * 128 + (sizeof(Out) == sizeof(In) ? 0 : (size_t)CB * ITEMS * sizeof(Out));
@@ -826,7 +626,6 @@ pdlgb300_error scan_chain_typed(ScanArgs g, cudaStream_t s) {
 }
 
 template <class In, class Out> constexpr int64_t chain_chunk() {
-  if constexpr (wchain_ok<In, Out>()) return 32 * (128 / sizeof(In));  // a warp's unit
   if constexpr (chain_ok<In, Out>()) return (int64_t)chain_threads<In, Out>() * (128 / sizeof(In));
   return 0;
 }

@@ -2,6 +2,7 @@
 bench makes), shared by the real-PDL fixture script and the tests that
 compare against its fixtures.  numpy's PCG64 streams give the same bytes on
 every platform, and the fixtures record each input's SHA-256 to prove it."""
+import functools
 import hashlib
 
 import numpy as np
@@ -36,10 +37,58 @@ def exp_portable(x: np.ndarray) -> np.ndarray:
     return np.ldexp(p, e.astype(np.int32))
 
 
+LN2 = 0.6931471805599453
+
+
+def log_portable(x: np.ndarray) -> np.ndarray:
+    """Natural log of positive normal float64 x with the same bits on every
+    platform: only IEEE float64 adds, multiplies, divides and frexp.
+    x = m 2^e with m in [sqrt(1/2), sqrt(2)); log m = 2 atanh(s),
+    s = (m - 1)/(m + 1), |s| < 0.1716, from the odd series to s^23 (each
+    term below 1e-18 of the sum after that)."""
+    m, e = np.frexp(np.asarray(x, dtype=np.float64))
+    small = m < 0.7071067811865476
+    m = np.where(small, m * 2.0, m)
+    e = np.where(small, e - 1, e).astype(np.float64)
+    s = (m - 1.0) / (m + 1.0)
+    s2 = s * s
+    p = np.full_like(s, 1.0 / 23.0)
+    for k in range(21, 0, -2):
+        p *= s2
+        p += 1.0 / k
+    return e * LN2 + 2.0 * s * p
+
+
+def normal_portable(rng: np.random.Generator, count: int) -> np.ndarray:
+    """count standard normal float64 values by Marsaglia's polar method from
+    rng.random() doubles (exact integer-derived values) and log_portable:
+    the same values on every platform, unlike numpy's ziggurat, whose
+    rejection step calls the platform's libm."""
+    out = np.empty(count)
+    got = 0
+    while got < count:
+        k = (count - got) // 2 + 1024
+        u = 2.0 * rng.random(k) - 1.0
+        v = 2.0 * rng.random(k) - 1.0
+        s = u * u + v * v
+        keep = (s > 0.0) & (s < 1.0)
+        u, v, s = u[keep], v[keep], s[keep]
+        f = np.sqrt(-2.0 * log_portable(s) / s)
+        z = np.empty(2 * len(s))
+        z[0::2] = u * f
+        z[1::2] = v * f
+        take = min(len(z), count - got)
+        out[got:got + take] = z[:take]
+        got += take
+    return out
+
+
+@functools.lru_cache(maxsize=1)
 def c5(rows=4096, n=65536, long_n=1 << 27):
     """float32 (65536, 4096) and one row of 2^27: lognormal(0, 4) magnitudes
     (exp(4 z), z standard normal), random sign, 1 % float's default badvalue,
-    seed 7."""
+    seed 7.  The last result is cached (about 40 s to make): callers must not
+    modify the arrays."""
     rng = np.random.default_rng(7)
 
     def gen(count):
@@ -47,7 +96,7 @@ def c5(rows=4096, n=65536, long_n=1 << 27):
         step = 1 << 24
         for s in range(0, count, step):                 # bounded temporaries
             m = min(step, count - s)
-            z = rng.standard_normal(m, dtype=np.float32)
+            z = normal_portable(rng, m).astype(np.float32)
             out[s:s + m] = exp_portable(np.float32(4.0) * z)
         out *= np.where(rng.random(count, dtype=np.float32) < 0.5, np.float32(-1), np.float32(1))
         out[rng.random(count, dtype=np.float32) < 0.01] = F32_BAD

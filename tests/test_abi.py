@@ -191,7 +191,7 @@ def test_error_table_format():
     with pytest.raises(P.PDLError) as ei:
         lib_redodims("plus", [Z("double", 3), Z("double", 4)])
     msg = str(ei.value)
-    assert msg.startswith("plus(a,b,c): parameter 'b': Mismatched implicit broadcast dimension 0")
+    assert msg.startswith("PDL::Ops::plus(a,b,c): parameter 'b': Mismatched implicit broadcast dimension 0")
     assert "There are 3 PDLs in the expression; 1 broadcast dim." in msg
     assert "   #  0 (normal):        3" in msg
     assert "   #  2 (null)" in msg
@@ -223,3 +223,12 @@ def test_options_roundtrip():
         assert L.pdlgb300_get_option(A.OPT_MATMULT_MODE) == m
     assert L.pdlgb300_set_option(A.OPT_MATMULT_MODE, 7).error
     A.check(L.pdlgb300_set_option(A.OPT_MATMULT_MODE, old))
+
+
+def test_op_package_names_the_defining_package():
+    """PDL names ops by their package-qualified pp_def name in its errors."""
+    L = A.lib()
+    assert L.pdlgb300_op_package(b"plus") == b"PDL::Ops::"
+    assert L.pdlgb300_op_package(b"sumover") == b"PDL::Ufunc::"
+    assert L.pdlgb300_op_package(b"matmult") == b"PDL::Primitive::"
+    assert L.pdlgb300_op_package(b"sumover_mult_plus") == b""
