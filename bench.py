@@ -28,6 +28,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -84,6 +85,36 @@ def op_bytes(op, n=N0, rows=N1, isz=8, osz=8):
     if op.startswith("cumu") or op.startswith("dcumu"):
         return rows * n * (isz + osz)
     return rows * n * isz + rows * (8 if op.endswith("_ind") else osz)
+
+
+FIXTURES = ROOT / "tests" / "golden" / "pdl_fixtures.npz"
+
+
+def pdl_fixtures():
+    """The reference PDL's own outputs on these seeded inputs (made by
+    tests/golden/make_pdl_fixtures.py), or None."""
+    try:
+        return np.load(FIXTURES)
+    except OSError:
+        return None
+
+
+def errs(got, want):
+    """Max elementwise relative error (|want| the denominator; the absolute
+    error where want is 0), normwise error, and whether the bits are equal.
+    NaN positions must agree; BAD (NaN or badvalue) positions are compared as
+    values."""
+    got, want = np.ascontiguousarray(got), np.ascontiguousarray(want)
+    exact = got.dtype == want.dtype and got.shape == want.shape and \
+        np.array_equal(got.view(np.uint8), want.view(np.uint8))
+    g, w = got.astype(np.float64), want.astype(np.float64)
+    nan = np.isnan(g) & np.isnan(w)
+    d = np.where(nan, 0.0, np.abs(g - w))
+    den = np.abs(np.where(nan, 0.0, w))
+    rel = np.where(den > 0, d / np.where(den > 0, den, 1.0), d)
+    nw = float(np.linalg.norm(d.ravel()) / max(np.linalg.norm(den.ravel()), 1e-300))
+    return {"max_rel_err": float(np.nanmax(rel)) if rel.size else 0.0, "normwise_err": nw,
+            "bit_exact": bool(exact)}
 
 
 class Clocks:
@@ -266,6 +297,7 @@ def run_ours(args, rank, world):
         result["inner_c3"] = bench_inner(args, P, torch, stream, hbm)
         result["expr"] = bench_expr(args, P, torch, stream, hbm)
         result["sort"] = bench_sort(args, P, torch, stream, hbm)
+        result["fastraw"] = bench_fastraw(args, P, torch, stream)
     if rank == 0 and not args.no_cpu:
         result["cpu_baseline"] = cpu_baseline(args, mat)
     return result
@@ -397,6 +429,22 @@ def c5_accuracy(P, xs, arrays):
             res[key][mode] = {"max_rel_err": float(rel.max()),
                               "max_normwise_err": float((err / np.maximum(scale[good], 1e-300)).max())}
     res["reference_point"] = "float64 GPU path (d-variants), itself checked against the CPU oracle in tests"
+    fx = pdl_fixtures()
+    if fx is not None and mat.shape[0] == 4096:
+        vs = {}
+        for j, x in enumerate(xs):
+            nm = "c5m" if j == 0 else "c5r"
+            where = "matrix" if j == 0 else "row"
+            for op in ("sumover", "average", "dsumover", "daverage"):
+                vs[f"{op}[{where}]"] = errs(getattr(P, op)(x).numpy().reshape(-1),
+                                            fx[f"{nm}/{op}"].reshape(-1))
+            got = P.cumusumover(x).numpy()
+            got = got[::64, ::128] if j == 0 else got.reshape(1, -1)[:, ::65536]
+            vs[f"cumusumover[{where}]"] = errs(got, fx[f"{nm}/cumusumover/sample"])
+        res["vs_reference_pdl"] = vs
+        res["vs_reference_pdl_note"] = ("the reference PDL 2.106's own outputs on the same inputs "
+                                        "(plain float32 loops for sumover/average/cumusumover; "
+                                        "their error, not ours, dominates these figures)")
     return res
 
 
@@ -429,7 +477,16 @@ def run_family(args, P, torch, stream, hbm):
     step_bytes = sum(op_bytes(op) for op in UFUNC_OPS)
     ms = total / args.steps
     op_ms = {op: statistics.mean(per_op[j]) for j, op in enumerate(UFUNC_OPS)}
-    return {"workload": FAMILY, "ops": UFUNC_OPS,
+    fx, err = pdl_fixtures(), {}
+    if fx is not None:
+        for op in UFUNC_OPS:
+            got = outs[op].numpy()
+            if op == "cumusumover":
+                err[op] = errs(got[::32, ::16], fx["c1/cumusumover/sample"])
+                err[op]["sample"] = "rows ::32, positions ::16"
+            elif f"c1/{op}" in fx.files:
+                err[op] = errs(got, fx[f"c1/{op}"])
+    return {"workload": FAMILY, "ops": UFUNC_OPS, "error_vs_reference_pdl": err,
             "l2": f"inputs rotate over {NCOPIES} device copies ({NCOPIES * N0 * N1 * 8 >> 20} MiB)",
             "value": step_bytes / (ms * 1e-3) / 1e9, "unit": "GB/s", "ms_per_step": ms,
             "frac_of_hbm": step_bytes / (ms * 1e-3) / 1e9 / hbm,
@@ -472,6 +529,11 @@ def bench_matmult(args, P, torch, stream, bf16, peak_kind):
             err = max(err, float(np.max(diff) / np.max(np.abs(ref))))
         out[name] = {"tflops": flops / (ms * 1e-3) / 1e12, "ms": ms, "kernel": kern,
                      "max_normwise_rel_err": err}
+        fx = pdl_fixtures()
+        if fx is not None and NB == 16:
+            # the reference PDL's float32 matmult: batches 0 and 11, rows (h) ::256
+            e = errs(cn[[0, 11]][:, ::256, :], fx["c3m/sample"])
+            out[name]["error_vs_reference_pdl"] = {k: v for k, v in e.items() if k != "bit_exact"}
     P.set_matmult_mode(P.MATMULT_BF16X6)
     out["config"] = f"a(t=1024,h=2048) x b(w=2048,t=1024), batch {NB}, float32 N(0,1) seed 4"
     out["speedup_bf16x6_vs_simt"] = out["bf16x6"]["tflops"] / out["simt_fp32"]["tflops"]
@@ -542,6 +604,22 @@ def bench_c2(args, P, torch, stream):
         ms_g = time_op(torch, stream, lambda: P.sumover(P.plus(P.mult(x, y), x)), 3)
         out[name].update({"expr_generic_ms": ms_e, "eager_chain_ms": ms_g,
                           "expr_generic_equals_tiled": same})
+        # output rows (dim 1) ::2048 against the reference PDL and in FP64
+        got = c.numpy()[::2048]
+        fx = pdl_fixtures()
+        if fx is not None:
+            out[name]["error_vs_reference_pdl"] = errs(got, fx["c2i/sample" if name == "int32"
+                                                             else "c2f/sample"])
+        av, bv = ha[::2048, 0, :].astype(np.float64), hb[0].astype(np.float64)   # (4,256), (512,256)
+        t = av[:, None, :] * bv[None, :, :] + av[:, None, :]
+        if badflag:
+            good = (ha[::2048, 0, :] != bad)[:, None, :] & (hb[0] != bad)[None, :, :]
+            ref = np.where(good, t, 0.0).sum(-1)
+            ref = np.where(good.any(-1), ref, float(bad))
+        else:
+            ref = t.sum(-1)
+        e64 = errs(got, ref)
+        out[name]["error_vs_fp64"] = {k: v for k, v in e64.items() if k != "bit_exact"}
     out["config"] = ("sumover(a*b+a): a (256,1,8192), b (256,512,1) -> (512,8192); "
                      "int32 U{-1000..1000} seed 2; float32 N(0,1) seed 3 with 2% BAD")
     out["bound"] = "int32 / fp32 pipe (3 ops per element evaluation, ~120 ops per byte)"
@@ -649,6 +727,7 @@ def bench_inner(args, P, torch, stream, hbm):
     a = rng.uniform(-1.0, 1.0, size=(cols, 4096))
     b = rng.uniform(-1.0, 1.0, size=(cols, 4096))
     x, y = P.pdl(a).to_device(), P.pdl(b).to_device()
+    a8, b8 = a[::8].copy(), b[::8].copy()
     del a, b
     c = P.inner(x, y)
     P.sync()
@@ -656,9 +735,17 @@ def bench_inner(args, P, torch, stream, hbm):
     ms = time_op(torch, stream, lambda: P.inner(x, y, c), args.mm_steps + 7)
     nbytes = 2 * 4096 * cols * 8 + cols * 8
     gbs = nbytes / (ms * 1e-3) / 1e9
-    return {"config": f"inner, float64 a,b dims (4096,{cols}) U[-1,1) seed 5 -> {cols}",
-            "ms": ms, "gbs": gbs, "frac_of_hbm": gbs / hbm, "kernel": kern,
-            "gflops": 2 * 4096 * cols / (ms * 1e-3) / 1e9}
+    res = {"config": f"inner, float64 a,b dims (4096,{cols}) U[-1,1) seed 5 -> {cols}",
+           "ms": ms, "gbs": gbs, "frac_of_hbm": gbs / hbm, "kernel": kern,
+           "gflops": 2 * 4096 * cols / (ms * 1e-3) / 1e9}
+    got = c.numpy()[::8]
+    fx = pdl_fixtures()
+    if fx is not None and cols == 65536:
+        res["error_vs_reference_pdl"] = errs(got, fx["c3i/sample"])
+        res["error_vs_reference_pdl"]["sample"] = "every 8th output"
+    ref = np.array([math.fsum(r) for r in a8 * b8])      # exactly rounded sums of the FP64 products
+    res["error_vs_exact_sum"] = {k: v for k, v in errs(got, ref).items() if k != "bit_exact"}
+    return res
 
 
 def bench_expr(args, P, torch, stream, hbm):
@@ -670,6 +757,8 @@ def bench_expr(args, P, torch, stream, hbm):
     a = rng.standard_normal((rows, 65536), dtype=np.float32)
     b = rng.standard_normal((rows, 65536), dtype=np.float32)
     x, y = P.pdl(a).to_device(), P.pdl(b).to_device()
+    sample = np.arange(0, rows, 64)
+    ref = ((a[sample].astype(np.float64) - b[sample]) ** 2).sum(-1)
     del a, b
     d = P.lazy(x) - y
     e = d * d
@@ -684,9 +773,12 @@ def bench_expr(args, P, torch, stream, hbm):
     ms_eager = time_op(torch, stream, eager, 3)
     nbytes = 2 * rows * 65536 * 4 + rows * 4
     gbs = nbytes / (ms * 1e-3) / 1e9
+    e64 = errs(c.numpy()[sample], ref)
     return {"config": f"sumover((a-b)*(a-b)), float32 a,b dims (65536,{rows}) N(0,1) seed 8 -> {rows}",
             "ms": ms, "gbs": gbs, "frac_of_hbm": gbs / hbm, "op": op,
-            "eager_ms": ms_eager, "speedup_vs_eager": ms_eager / ms}
+            "eager_ms": ms_eager, "speedup_vs_eager": ms_eager / ms,
+            "error_vs_fp64": {"max_rel_err": e64["max_rel_err"], "normwise_err": e64["normwise_err"],
+                              "sample": "every 64th output, FP64 from the float32 inputs"}}
 
 
 def bench_sort(args, P, torch, stream, hbm):
@@ -710,12 +802,68 @@ def bench_sort(args, P, torch, stream, hbm):
     xs = P.pdl(np.ascontiguousarray(a[:8192]))
     n = os.cpu_count() or 1
     t0 = time.perf_counter()
-    O.run("medover", [xs], nthreads=n)
+    want = O.run("medover", [xs], nthreads=n)
     el = time.perf_counter() - t0
+    got = P.medover(x).numpy()[:8192]
+    want = want[0].numpy().reshape(got.shape)
+    out["medover"]["error_vs_oracle"] = errs(got, want)
+    out["medover"]["error_vs_oracle"]["sample"] = "the first 8192 rows"
     out["cpu_medover"] = {"rows_per_s": 8192 / el, "cores": n, "kind": "port",
                           "sample": "8192 of the 65536 rows"}
     out["bound"] = ("a warp per row: bitonic network in shared memory (the reference's "
                     "quicksort on the rows whose result could depend on the sort)")
+    # vector sorts: 512 planes of 2048 points in 3-D (float64, N(0,1), seed 11)
+    v = np.random.default_rng(11).standard_normal((512, 2048, 3))
+    xv = P.pdl(v).to_device()
+    vbytes = v.nbytes
+    for op in ("qsortvec", "qsortveci"):
+        r = getattr(P, op)(xv)
+        P.sync()
+        ms = time_op(torch, stream, lambda: getattr(P, op)(xv), 5)
+        want = O.run(op, [P.pdl(np.ascontiguousarray(v[:16]))], nthreads=n)[0].numpy()
+        out[op] = {"config": "float64 dims (3, 2048, 512): 512 planes of 2048 3-vectors, N(0,1) seed 11",
+                   "ms": ms, "planes_per_s": 512 / (ms * 1e-3), "gbs_in": vbytes / (ms * 1e-3) / 1e9,
+                   "kernel": "k_qsortvec_block",
+                   "error_vs_oracle": errs(r.numpy()[:16], want)}
+        del r
+    t0 = time.perf_counter()
+    O.run("qsortvec", [P.pdl(np.ascontiguousarray(v[:64]))], nthreads=n)
+    out["cpu_qsortvec"] = {"planes_per_s": 64 / (time.perf_counter() - t0), "cores": n,
+                           "kind": "port", "sample": "64 of the 512 planes"}
+    return out
+
+
+def bench_fastraw(args, P, torch, stream):
+    """FastRaw to device memory: a float32 file of 1 GiB (PDL dims
+    (65536, 4096), seeded N(0,1)) written by writefraw to the local temp
+    directory, then read straight into device memory by readfraw(device=True)
+    (file reads through two pinned staging buffers, the reads overlapping
+    the host-to-device copies) and by mapfraw + to_device (the file mapped,
+    one copy from the mapping).  The file was just written, so it is read
+    from the page cache: these time the host side and the link, not a disk."""
+    import tempfile
+    rows = 4096
+    a = np.random.default_rng(10).standard_normal((rows, 65536), dtype=np.float32)
+    nbytes = a.nbytes
+    out = {"config": f"float32 PDL dims (65536, {rows}), {nbytes >> 20} MiB, page cache warm"}
+    with tempfile.TemporaryDirectory() as td:
+        name = os.path.join(td, "c5f")
+        P.writefraw(P.pdl(a), name)
+        for how, fn in (("readfraw_device", lambda: P.readfraw(name, device=True)),
+                        ("mapfraw_to_device", lambda: P.mapfraw(name, ReadOnly=True).to_device())):
+            x = fn()
+            P.sync()
+            ts = []
+            for _ in range(3):
+                del x
+                t0 = time.perf_counter()
+                x = fn()
+                P.sync()
+                ts.append(time.perf_counter() - t0)
+            ok = bool(np.array_equal(x.numpy()[::997], a[::997]))
+            del x
+            out[how] = {"s": statistics.median(ts), "gbs": nbytes / statistics.median(ts) / 1e9,
+                        "sampled_rows_equal": ok}
     return out
 
 

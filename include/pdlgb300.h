@@ -206,6 +206,15 @@ pdlgb300_error pdlgb300_run_pctover(pdlgb300_ndarray *a, pdlgb300_ndarray *p,
 pdlgb300_error pdlgb300_run_oddpctover(pdlgb300_ndarray *a, pdlgb300_ndarray *p,
                                        pdlgb300_ndarray *b);
 pdlgb300_error pdlgb300_run_modeover(pdlgb300_ndarray *data, pdlgb300_ndarray *out);
+/* lib/PDL/Ufunc.pd:1115-1231, the vector sorts, with the reference's vector
+ * quicksort (lexicographic pdl_cmpvec, middle vector as pivot) so that
+ * vectors comparing equal keep the reference's order:
+ *   qsortvec a(n,m); [o]b(n,m)         -- vectors with a bad component to
+ *                                          the end, the first of them last
+ *   qsortveci a(n,m); indx [o]indx(m)  -- the same order as positions
+ * An empty a leaves the outputs unwritten, as the reference does.       */
+pdlgb300_error pdlgb300_run_qsortvec(pdlgb300_ndarray *a, pdlgb300_ndarray *b);
+pdlgb300_error pdlgb300_run_qsortveci(pdlgb300_ndarray *a, pdlgb300_ndarray *indx);
 /* lib/PDL/IO/FastRaw.pm:202-323: FastRaw files.  The header ("<name>.hdr"
  * unless `header` names one) holds "<type id>\n<ndims>\n<dim0> <dim1> ...\n".
  *   pdlgb300_fraw_header  -- shape and type x from the header (_read_frawhdr)

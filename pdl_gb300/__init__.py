@@ -19,12 +19,12 @@ from .ndarray import (  # noqa: F401
     and2, divide, eq, ge, gt, le, lt, minus, ne, or2, shiftleft, shiftright, xor, xor2,
     andover, bandover, borover, bxorover, firstnonzeroover, orover, xorover, zcover,
     cumuprodover, dcumuprodover, minmaximum, minmaxover, qsort, qsorti, medover, oddmedover,
-    modeover, pctover, oddpctover)
+    modeover, pctover, oddpctover, qsortvec, qsortveci)
 from .whole import (  # noqa: F401
     all, and_, any, avg, band, bor, bxor, davg, dprod, dsum, max, median, min, mode, oddmedian,
     oddpct, or_, pct, prod, sum, xorall, zcheck)
 from .lazy import Lazy, lazy  # noqa: F401
-from .fastraw import gluefraw, readfraw, writefraw  # noqa: F401
+from .fastraw import gluefraw, mapfraw, readfraw, writefraw  # noqa: F401
 from ._abi import MATMULT_BF16X3, MATMULT_BF16X6, MATMULT_SIMT_EXACT, MATMULT_SIMT_FP32  # noqa: F401
 
 # `from pdl_gb300 import *` leaves Python's builtins alone: the whole-array

@@ -103,6 +103,8 @@ SIGNATURES = {
     "pdlgb300_run_pctover": (Error, [P, P, P]),
     "pdlgb300_run_oddpctover": (Error, [P, P, P]),
     "pdlgb300_run_modeover": (Error, [P, P]),
+    "pdlgb300_run_qsortvec": (Error, [P, P]),
+    "pdlgb300_run_qsortveci": (Error, [P, P]),
     "pdlgb300_fraw_header": (Error, [C.c_char_p, C.c_char_p, P]),
     "pdlgb300_readfraw_into": (Error, [C.c_char_p, P]),
     "pdlgb300_writefraw": (Error, [P, C.c_char_p, C.c_char_p]),

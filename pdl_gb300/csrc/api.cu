@@ -119,7 +119,8 @@ enum OpId {
   O_SHIFTLEFT, O_SHIFTRIGHT, O_OR2, O_AND2, O_XOR,
   O_ANDOVER, O_OROVER, O_XOROVER, O_ZCOVER, O_BANDOVER, O_BOROVER, O_BXOROVER,
   O_FIRSTNONZEROOVER, O_CUMUPRODOVER, O_DCUMUPRODOVER, O_MINMAXIMUM,
-  O_QSORT, O_QSORTI, O_MEDOVER, O_ODDMEDOVER, O_PCTOVER, O_ODDPCTOVER, O_MODEOVER, O_NOPS
+  O_QSORT, O_QSORTI, O_MEDOVER, O_ODDMEDOVER, O_PCTOVER, O_ODDPCTOVER, O_MODEOVER,
+  O_QSORTVEC, O_QSORTVECI, O_NOPS
 };
 
 // binary ops (a(); b(); [o]c(); int swap) and their kernel codes
@@ -157,6 +158,7 @@ const char *const I_THW[] = {"t", "h", "w"};
 const char *const N_AI[] = {"a", "indx"};
 const char *const N_APB[] = {"a", "p", "b"};
 const char *const N_DO[] = {"data", "out"};
+const char *const I_NM[] = {"n", "m"};
 
 const int32_t RD_10[] = {1, 0}, RD_11[] = {1, 1}, RD_000[] = {0, 0, 0},
               RD_110[] = {1, 1, 0}, RD_222[] = {2, 2, 2}, RD_1110[] = {1, 1, 1, 0};
@@ -168,6 +170,7 @@ const int32_t PT_L[] = {-1, PDLGB300_L}, PT_D[] = {-1, PDLGB300_D},
 const int32_t RD_10000[] = {1, 0, 0, 0, 0}, F_MM4[] = {0, OUT_C, OUT_C, OUT_T, OUT_T},
               PT_MM4[] = {-1, -1, -1, PDLGB300_IND, PDLGB300_IND};
 const int32_t RD_100[] = {1, 0, 0}, F_APB[] = {0, 0, OUT_C};
+const int32_t RD_22[] = {2, 2}, RD_21[] = {2, 1}, ID_NMNM[] = {0, 1, 0, 1}, ID_NMM[] = {0, 1, 1};
 const int32_t ID_N0[] = {0}, ID_NN[] = {0, 0}, ID_NNN[] = {0, 0, 0},
               ID_MM[] = {0, 1, 2, 0, 2, 1}, ID_NONE[] = {0};
 
@@ -225,6 +228,9 @@ const pdlgb300_vtable VT[O_NOPS] = {
     {"pctover", 3, 2, 1, 0, N_APB, RD_100, F_APB, PT_NONE, ID_NNN, I_N, REALTYPES},
     {"oddpctover", 3, 2, 1, 0, N_APB, RD_100, F_APB, PT_NONE, ID_NNN, I_N, REALTYPES},
     {"modeover", 2, 1, 1, 0, N_DO, RD_10, F_C, PT_NONE, ID_N0, I_N, INTTYPES},
+    // lib/PDL/Ufunc.pd:1115-1231: a(n,m); [o]b(n,m) / indx [o]indx(m)
+    {"qsortvec", 2, 1, 2, 0, N_AB, RD_22, F_C, PT_NONE, ID_NMNM, I_NM, REALTYPES},
+    {"qsortveci", 2, 1, 2, 0, N_AI, RD_21, F_T, PT_N, ID_NMM, I_NM, REALTYPES},
 };
 
 int op_of(const pdlgb300_vtable *vt) {
@@ -1247,6 +1253,62 @@ pdlgb300_error dispatch_sortred(RunCtx &c, int kind) {
   return e;
 }
 
+pdlgb300_error dispatch_qsortvec(RunCtx &c, bool ind) {
+  const Brc &b = c.b;
+  VecSortArgs g;
+  memset(&g, 0, sizeof g);
+  const int which[2] = {0, 1};
+  g.L = collapse(b, 2, which);
+  g.rows = g.L.total;
+  g.n = b.ind_sizes[0];
+  g.m = b.ind_sizes[1];
+  g.inc_an = b.inc_sizes[0][0];
+  g.inc_am = b.inc_sizes[0][1];
+  g.inc_bn = ind ? 0 : b.inc_sizes[1][0];
+  g.inc_bm = ind ? b.inc_sizes[1][0] : b.inc_sizes[1][1];
+  g.a = c.dev[0];
+  g.b = c.dev[1];
+  g.bad = c.bvalflag;
+  g.abad = bad_bits(&c.v[0]);
+  g.abad_isnan = bad_isnan(&c.v[0]);
+  g.obad = bad_bits(&c.v[1]);
+  const int dt = c.v[0].datatype;
+  tl_info.rows = g.rows;
+  tl_info.n = g.n * g.m;
+  tl_info.bytes = (double)g.rows * g.n * g.m * TSIZES[dt] +
+                  (double)g.rows * (ind ? g.m * 8 : g.n * g.m * TSIZES[dt]);
+  // qsort_returnempty (Ufunc.pd:1038): nothing to do for an empty a
+  if (g.rows == 0 || g.n == 0 || g.m == 0) return ok();
+  int dev = 0, optin = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  const size_t limit = (size_t)std::max(0, optin - 1024);  // (the block's static shared words)
+  void *scratch = nullptr;
+  if (qsortvec_smem_bytes(g.n, g.m, (int)TSIZES[dt]) > limit) {
+    const size_t vbytes = ((size_t)g.rows * g.n * g.m * TSIZES[dt] + 15) & ~(size_t)15;
+    RET_IF(dalloc(vbytes + (size_t)g.rows * g.m * sizeof(int64_t), &scratch));
+    g.scratch = scratch;
+    g.iscratch = (int64_t *)((char *)scratch + vbytes);
+  }
+  int *w = nullptr;
+  pdlgb300_error e = status_word(&w);
+  g.err = w;
+  int hs = 0;
+  if (!e.error) {
+    cudaError_t ce = cudaMemsetAsync(w, 0, sizeof(int), g_stream);
+    if (ce != cudaSuccess) e = err(PDLGB300_EFATAL, "clearing the status word: %s", cudaGetErrorString(ce));
+  }
+  if (!e.error) e = launch_qsortvec(ind, dt, g, limit, g_stream);
+  if (!e.error) {
+    cudaError_t ce = cudaMemcpyAsync(&hs, w, sizeof(int), cudaMemcpyDeviceToHost, g_stream);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(g_stream);
+    if (ce != cudaSuccess) e = err(PDLGB300_EFATAL, "%s: %s", c.vt->name, cudaGetErrorString(ce));
+  }
+  if (scratch) cudaFreeAsync(scratch, g_stream);
+  if (!e.error && hs) e = err(PDLGB300_EFATAL, "%s: a sort scan left its range", c.vt->name);
+  return e;
+}
+
 pdlgb300_error dispatch_biop(RunCtx &c, int which_op) {
   BiopArgs g;
   memset(&g, 0, sizeof g);
@@ -1440,6 +1502,8 @@ pdlgb300_error dispatch(RunCtx &c, const int64_t *) {
     case O_PCTOVER: return dispatch_sortred(c, SR_PCT);
     case O_ODDPCTOVER: return dispatch_sortred(c, SR_ODDPCT);
     case O_MODEOVER: return dispatch_sortred(c, SR_MODE);
+    case O_QSORTVEC: return dispatch_qsortvec(c, false);
+    case O_QSORTVECI: return dispatch_qsortvec(c, true);
     case O_CUMUPRODOVER: return dispatch_cumusum(c, 2);
     case O_DCUMUPRODOVER: return dispatch_cumusum(c, 3);
     case O_INNER: return dispatch_inner(c);
@@ -1859,6 +1923,8 @@ RUN2(qsorti, O_QSORTI)
 RUN2(medover, O_MEDOVER)
 RUN2(oddmedover, O_ODDMEDOVER)
 RUN2(modeover, O_MODEOVER)
+RUN2(qsortvec, O_QSORTVEC)
+RUN2(qsortveci, O_QSORTVECI)
 
 pdlgb300_error pdlgb300_run_pctover(pdlgb300_ndarray *a, pdlgb300_ndarray *p, pdlgb300_ndarray *b) {
   pdlgb300_ndarray *q[3] = {a, p, b};

@@ -141,6 +141,24 @@ struct SortArgs {
 };
 pdlgb300_error launch_sortred(int kind, int dt, const SortArgs &g, cudaStream_t s);
 
+// qsortvec / qsortveci: a(n,m) -> b(n,m) or indx(m)
+struct VecSortArgs {
+  const char *a;      // element (0,0) of a
+  char *b;            // element (0) of the output
+  int64_t n, m, rows;
+  int64_t inc_an, inc_am, inc_bn, inc_bm;
+  Loop L;             // pdl 0 a, 1 the output
+  int bad;
+  uint64_t abad, obad;
+  int abad_isnan;
+  void *scratch;      // rows x n x m values (the one-thread-per-row kernel)
+  int64_t *iscratch;  // rows x m positions (the same)
+  int *err;           // bit 0: a scan left its range (never expected)
+};
+size_t qsortvec_smem_bytes(int64_t n, int64_t m, int tsize);
+pdlgb300_error launch_qsortvec(bool ind, int dt, const VecSortArgs &g, size_t smem_limit,
+                               cudaStream_t s);
+
 struct ConvArgs {
   const char *src;
   char *dst;

@@ -73,6 +73,23 @@ __global__ void __launch_bounds__(FT) k_fused_outer(const FusedArgs g) {
   __shared__ T sa[FN][FK + 1];
   __shared__ T sb[FN][FJ + 1];
   __shared__ T sd[DA ? 1 : FN][DA ? 1 : FK + 1];
+  // float32 in bad-value mode with d = a: each staged value once -- zeroed where bad,
+  // b's goodness as 0/1, good bits of each column over the slab (a ballot:
+  // the staging lanes are the slab's i), the slab's largest magnitudes --
+  // so that a slab whose products cannot reach the badvalue costs a pair
+  // three float operations.  Rows of 16-byte chunks, chunk c of row i at
+  // c ^ (i & 15), read four values at a time.
+  // (with a separate d the copies would pass the 48 KB of static shared
+  // memory; that case keeps the per-thread tests below)
+  constexpr bool FPB = BAD && DA && std::is_same_v<T, float>;
+  constexpr int ZN = FPB ? FN : 1, ZK = FPB ? FK : 4, ZJ = FPB ? FJ : 4;
+  __shared__ __align__(16) T za[ZN][ZK];
+  __shared__ __align__(16) T zd[(FPB && !DA) ? FN : 1][(FPB && !DA) ? FK : 4];
+  __shared__ __align__(16) T zb[ZN][ZJ];
+  __shared__ __align__(16) T zg[ZN][ZJ];
+  __shared__ uint32_t mka[FPB ? FK : 1], mkb[FPB ? FJ : 1];
+  __shared__ int s_max[2][3], s_fin[2];  // per slab parity: max |a|, |b|, |d| (float bits)
+  auto swz = [](int i, int v) { return (((v >> 2) ^ (i & 15)) << 2) | (v & 3); };
   const int tid = threadIdx.x, tj = tid % 16, tk = tid / 16;
   const int64_t J = g.L.size[g.jdim], K = g.L.size[g.kdim];
   const int64_t j0 = (int64_t)blockIdx.x * FJ, k0 = (int64_t)blockIdx.y * FK;
@@ -95,23 +112,134 @@ __global__ void __launch_bounds__(FT) k_fused_outer(const FusedArgs g) {
       acc[x][y] = FA::zero();
       cnt[x][y] = false;
     }
-  for (int64_t i0 = 0; i0 < g.n; i0 += FN) {
+  // Compensated float32: the pairs of one slab are summed plainly (FN
+  // values, error below FN ulps of their magnitudes' sum), and each slab's
+  // sum is added to the compensated accumulator: a pair costs one add, not
+  // the seven of a compensated add.
+  constexpr bool SLAB = std::is_same_v<typename FA::A, float2>;
+  T part[4][4];
+  if (FPB && tid < 2) {
+    s_max[tid][0] = s_max[tid][1] = s_max[tid][2] = 0;
+    s_fin[tid] = 1;
+  }
+  int par = 0;
+  for (int64_t i0 = 0; i0 < g.n; i0 += FN, par ^= 1) {
     uint32_t gma[4] = {0, 0, 0, 0}, gmb[4] = {0, 0, 0, 0};  // fast path: good bits of the slab
+    if constexpr (SLAB) {
+#pragma unroll
+      for (int y = 0; y < 4; y++)
+#pragma unroll
+        for (int x = 0; x < 4; x++) part[y][x] = (T)0;
+    }
     __syncthreads();
     // stage: FN x FK of a (and d), FN x FJ of b; i fastest across threads
+    float ma = 0.0f, mb = 0.0f, md = 0.0f;
+    bool sfin = true;
+    if (FPB && tid == 0) {
+      // the other parity's flags were read before this slab began
+      s_max[par ^ 1][0] = s_max[par ^ 1][1] = s_max[par ^ 1][2] = 0;
+      s_fin[par ^ 1] = 1;
+    }
     for (int idx = tid; idx < FN * FK; idx += FT) {
       int i = idx % FN, k = idx / FN;
       int64_t gi = i0 + i, gk = k0 + k;
       bool in = gi < g.n && gk < K;
-      sa[i][k] = in ? A[gi * g.inc_a + gk * a_k] : (T)0;
-      if constexpr (!DA) sd[i][k] = in ? D[gi * g.inc_d + gk * d_k] : (T)0;
+      const T av = in ? A[gi * g.inc_a + gk * a_k] : (T)0;
+      sa[i][k] = av;
+      T dv = av;
+      if constexpr (!DA) {
+        dv = in ? D[gi * g.inc_d + gk * d_k] : (T)0;
+        sd[i][k] = dv;
+      }
+      if constexpr (FPB) {
+        // (FN = 32 and FT a multiple of 32: a warp stages one column k,
+        // lane = i)
+        const bool good = in && !(g.fa && ba.is(av)) && !(g.fd && bd.is(dv));
+        const T a0 = good ? av : (T)0, d0 = good ? dv : (T)0;
+        za[i][swz(i, k)] = a0;
+        if constexpr (!DA) zd[i][swz(i, k)] = d0;
+        const uint32_t m = __ballot_sync(0xffffffffu, good);
+        if ((tid & 31) == 0) mka[k] = m;
+        sfin = sfin && isfinite(a0) && isfinite(d0);
+        ma = fmaxf(ma, fabsf(a0));
+        md = fmaxf(md, fabsf(d0));
+      }
     }
     for (int idx = tid; idx < FN * FJ; idx += FT) {
       int i = idx % FN, j = idx / FN;
       int64_t gi = i0 + i, gj = j0 + j;
-      sb[i][j] = (gi < g.n && gj < J) ? B[gi * g.inc_b + gj * b_j] : (T)0;
+      const bool in = gi < g.n && gj < J;
+      const T bv = in ? B[gi * g.inc_b + gj * b_j] : (T)0;
+      sb[i][j] = bv;
+      if constexpr (FPB) {
+        const bool good = in && !(g.fb && bb.is(bv));
+        const T b0 = good ? bv : (T)0;
+        zb[i][swz(i, j)] = b0;
+        zg[i][swz(i, j)] = good ? (T)1 : (T)0;
+        const uint32_t m = __ballot_sync(0xffffffffu, good);
+        if ((tid & 31) == 0) mkb[j] = m;
+        sfin = sfin && isfinite(b0);
+        mb = fmaxf(mb, fabsf(b0));
+      }
+    }
+    if constexpr (FPB) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        ma = fmaxf(ma, __shfl_xor_sync(0xffffffffu, ma, o));
+        mb = fmaxf(mb, __shfl_xor_sync(0xffffffffu, mb, o));
+        md = fmaxf(md, __shfl_xor_sync(0xffffffffu, md, o));
+      }
+      sfin = __all_sync(0xffffffffu, sfin);
+      if ((tid & 31) == 0) {
+        if (sfin) {
+          atomicMax(&s_max[par][0], __float_as_int(ma));
+          atomicMax(&s_max[par][1], __float_as_int(mb));
+          atomicMax(&s_max[par][2], __float_as_int(md));
+        } else {
+          atomicAnd(&s_fin[par], 0);
+        }
+      }
     }
     __syncthreads();
+    bool slab_fast = false;
+    if constexpr (FPB) {
+      // no product a*b nor sum a*b + d of the slab's good values can equal
+      // the intermediates' badvalue: finite values give no NaN, and the
+      // bound (rounded up, with a margin for the products' own rounding)
+      // stays below a finite badvalue's magnitude
+      if (s_fin[par]) {
+        const float bound = __fmaf_ru(__int_as_float(s_max[par][0]), __int_as_float(s_max[par][1]),
+                                      __int_as_float(s_max[par][2])) * (1.0f + 0x1p-20f);
+        slab_fast = bt.isnan_ || bound < fabsf((float)tbad);
+      }
+    }
+    if (slab_fast) {
+      if constexpr (FPB) {
+        const int iend = (int)(g.n - i0 < FN ? g.n - i0 : FN);
+        for (int i = 0; i < iend; i++) {
+          const float4 a4 = *reinterpret_cast<const float4 *>(&za[i][swz(i, tk * 4)]);
+          const float4 b4 = *reinterpret_cast<const float4 *>(&zb[i][swz(i, tj * 4)]);
+          const float4 g4 = *reinterpret_cast<const float4 *>(&zg[i][swz(i, tj * 4)]);
+          float4 d4 = a4;
+          if constexpr (!DA) d4 = *reinterpret_cast<const float4 *>(&zd[i][swz(i, tk * 4)]);
+          const float av[4] = {a4.x, a4.y, a4.z, a4.w}, bv[4] = {b4.x, b4.y, b4.z, b4.w};
+          const float gv[4] = {g4.x, g4.y, g4.z, g4.w}, dv[4] = {d4.x, d4.y, d4.z, d4.w};
+#pragma unroll
+          for (int y = 0; y < 4; y++)
+#pragma unroll
+            for (int x = 0; x < 4; x++) {
+              // the reference's two roundings, then the pair masked by b
+              const float u = __fadd_rn(__fmul_rn(av[x], bv[y]), dv[x]);
+              part[y][x] = __fmaf_rn(u, gv[y], part[y][x]);
+            }
+        }
+#pragma unroll
+        for (int y = 0; y < 4; y++)
+#pragma unroll
+          for (int x = 0; x < 4; x++)
+            cnt[y][x] = cnt[y][x] || (mka[tk * 4 + x] & mkb[tj * 4 + y]) != 0;
+      }
+    } else {
     const int iend = (int)(g.n - i0 < FN ? g.n - i0 : FN);
     for (int i = 0; i < iend; i++) {
       T av[4], bv[4], dv[4];
@@ -188,14 +316,19 @@ __global__ void __launch_bounds__(FT) k_fused_outer(const FusedArgs g) {
             gmb[x] |= (uint32_t)!xb[x] << i;
           }
           // (zeroed a and d make a pair with a bad a or d add 0 exactly; a bad
-          // b is selected away; one path for the whole warp: lanes hold 16
-          // different b groups, a branch on them would diverge)
+          // b is multiplied away -- u is finite here -- on one path for the
+          // whole warp: lanes hold 16 different b groups, a branch on them
+          // would diverge)
+          T bg[4];
+#pragma unroll
+          for (int y = 0; y < 4; y++) bg[y] = xb[y] ? (T)0 : (T)1;
 #pragma unroll
           for (int y = 0; y < 4; y++)
 #pragma unroll
             for (int x = 0; x < 4; x++) {
               const T u = op_add<T>(op_mul<T>(a0[x], b0[y]), d0[x]);
-              FA::add(acc[y][x], xb[y] ? (T)0 : u);
+              if constexpr (SLAB) part[y][x] = __fmaf_rn(u, bg[y], part[y][x]);
+              else FA::add(acc[y][x], xb[y] ? (T)0 : u);
             }
         } else {
           auto pairs = [&](auto tnan) {
@@ -222,10 +355,19 @@ __global__ void __launch_bounds__(FT) k_fused_outer(const FusedArgs g) {
 #pragma unroll
           for (int x = 0; x < 4; x++) {
             T u;
-            if (chain<T, BAD>(g, av[x], bv[y], dv[x], ba, bb, bd, bt, tbad, ubad, u))
-              FA::add(acc[y][x], u);
+            if (chain<T, BAD>(g, av[x], bv[y], dv[x], ba, bb, bd, bt, tbad, ubad, u)) {
+              if constexpr (SLAB && !BAD) part[y][x] = __fadd_rn(part[y][x], u);
+              else FA::add(acc[y][x], u);
+            }
           }
       }
+    }
+    }  // (the slab's values one thread at a time)
+    if constexpr (SLAB) {
+#pragma unroll
+      for (int y = 0; y < 4; y++)
+#pragma unroll
+        for (int x = 0; x < 4; x++) FA::add(acc[y][x], part[y][x]);
     }
     if constexpr (BAD) {
 #pragma unroll

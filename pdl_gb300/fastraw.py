@@ -7,6 +7,7 @@ from __future__ import annotations
 
 import ctypes as C
 import importlib
+import mmap
 import os
 from typing import Optional
 
@@ -98,3 +99,56 @@ def gluefraw(x: "N.ndarray", name: str, header: Optional[str] = None) -> None:
     hname = header or name + ".hdr"
     with open(hname, "w") as h:
         h.write(f"{t}\n{len(new_dims)}\n{' '.join(map(str, new_dims))}\n")
+
+
+def mapfraw(name: str, Dims=None, Datatype: Optional[int] = None, Creat: bool = False,
+            Trunc: bool = False, ReadOnly: bool = False, Header: Optional[str] = None) -> "N.ndarray":
+    """PDL::mapfraw (lib/PDL/IO/FastRaw.pm:393-418): the file mapped as the
+    ndarray's host memory (a shared mapping: set_data_by_file_map).  Dims and
+    Datatype give the shape instead of the header (Datatype defaults to
+    double); Creat creates the file and writes its header; Creat or Trunc
+    sizes the file to the data, zero-filled; ReadOnly maps it read-only.
+
+    On the GPU: to_device() copies the mapped bytes into a device mirror;
+    results an op writes there reach the file when the ndarray is brought
+    back to the host (to_host(), numpy()), because the host memory is the
+    mapping.  A read-only map is refused as an op's output, as PDL refuses a
+    read-only output."""
+    if Dims is not None:
+        t = A.D if Datatype is None else int(Datatype)
+        dims = tuple(int(d) for d in Dims)
+    else:
+        t, dims = read_header(name, Header)
+    if t not in N.NP_DTYPES:
+        raise PDLError(A.EUSERERROR, f"mapfraw: type {t} is not on this path")
+    nbytes = int(np.prod(dims, dtype=np.int64)) * np.dtype(N.NP_DTYPES[t]).itemsize if dims \
+        else np.dtype(N.NP_DTYPES[t]).itemsize
+    flags = os.O_RDONLY if ReadOnly else os.O_RDWR
+    if Creat:
+        flags |= os.O_CREAT
+    try:
+        fd = os.open(name, flags, 0o644)
+    except OSError as e:
+        raise PDLError(A.EUSERERROR, f"Error opening file '{name}': {e.strerror}") from None
+    try:
+        if Creat or Trunc:
+            os.ftruncate(fd, 0)
+            os.ftruncate(fd, nbytes)
+        size = os.fstat(fd).st_size
+        if size < nbytes:
+            raise PDLError(A.EUSERERROR, f"mapfraw: '{name}' has {size} bytes, the ndarray needs {nbytes}")
+        if nbytes:
+            mm = mmap.mmap(fd, nbytes, mmap.MAP_SHARED,
+                           mmap.PROT_READ if ReadOnly else mmap.PROT_READ | mmap.PROT_WRITE)
+            host = np.frombuffer(mm, dtype=np.uint8)
+        else:
+            host = np.zeros(1, np.uint8)
+    finally:
+        os.close(fd)
+    st = N.Storage(nbytes, host=host)
+    st.readonly = bool(ReadOnly)
+    x = N.ndarray(st, t, dims)
+    if Creat:
+        with open(Header or name + ".hdr", "w") as f:
+            f.write(f"{t}\n{len(dims)}\n{' '.join(map(str, dims))}\n")
+    return x

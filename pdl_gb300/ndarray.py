@@ -49,6 +49,7 @@ class Storage:
         self.host = host          # flat uint8 view or typed array
         self.dev = dev            # device pointer (int) or None
         self.fresh = "host" if host is not None else "dev"
+        self.readonly = False     # host memory that must not be written (a read-only file map)
 
     def host_ptr(self) -> int:
         return self.host.ctypes.data
@@ -71,6 +72,8 @@ class Storage:
         if self.host is None:
             self.host = np.empty(max(self.nbytes, 1), dtype=np.uint8)
         if self.fresh == "dev":
+            if self.readonly:
+                raise PDLError(A.EUSERERROR, "device data cannot be written back to a read-only map")
             if self.nbytes:
                 check(lib().pdlgb300_to_host(self.host.ctypes.data, self.dev, self.nbytes))
             self.fresh = "both"
@@ -134,6 +137,14 @@ class ndarray:
     @property
     def on_device(self) -> bool:
         return self.storage.dev is not None and self.storage.fresh in ("dev", "both")
+
+    # -- read-only (PDL's readonly / is_readonly; a read-only file map is always)
+    def readonly(self) -> "ndarray":
+        self._readonly = True
+        return self
+
+    def is_readonly(self) -> bool:
+        return getattr(self, "_readonly", False) or self.storage.readonly
 
     # -- bad values (lib/PDL/Bad.pd)
     def badflag(self, flag: Optional[bool] = None):
@@ -369,6 +380,8 @@ class ndarray:
     def medover(self, out=None): return medover(self, out)
     def oddmedover(self, out=None): return oddmedover(self, out)
     def modeover(self, out=None): return modeover(self, out)
+    def qsortvec(self, out=None): return qsortvec(self, out)
+    def qsortveci(self, out=None): return qsortveci(self, out)
     def pctover(self, p, out=None): return pctover(self, p, out)
     def oddpctover(self, p, out=None): return oddpctover(self, p, out)
     def median(self): return self.flat().medover()
@@ -516,6 +529,13 @@ def _run(vtname: str, inputs, outputs, other=None):
     vt = L.pdlgb300_get_vtable(vtname.encode())
     if not vt:
         raise PDLError(A.EUSERERROR, f"unknown op {vtname}")
+    for k, o in enumerate(outputs):
+        # pdl__transtype_select (lib/PDL/Core/pdlapi.c:1191-1194)
+        if o is not None and o.is_readonly():
+            j = len(inputs) + k
+            raise PDLError(A.EUSERERROR, f"{L.pdlgb300_op_package(vtname.encode()).decode()}{vtname} "
+                                         f"error: output parameter {vt.contents.par_names[j].decode()} "
+                                         "is read-only")
     use_dev = any(x.on_device for x in inputs) or any(
         o is not None and o.on_device for o in outputs)
     descs = [x._desc(use_dev) for x in inputs]
@@ -605,6 +625,8 @@ qsorti = _red("qsorti")
 medover = _red("medover")
 oddmedover = _red("oddmedover")
 modeover = _red("modeover")
+qsortvec = _red("qsortvec")
+qsortveci = _red("qsortveci")
 
 
 def pctover(a, p, out=None) -> "ndarray":

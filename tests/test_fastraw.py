@@ -122,3 +122,68 @@ def test_gluefraw_lower_dims_compare_like_the_reference(tmp_path):
     P.writefraw(P.pdl(np.zeros((2, 4, 3, 2))), cube)         # lower dims (2, 3, 4)
     with pytest.raises(P.PDLError, match="Mismatched implicit broadcast dimension 0: size 2 vs. 3"):
         P.gluefraw(P.pdl(np.zeros((3, 2))), cube)
+
+
+# ---- files written by the reference PDL's own writefraw
+# (tests/golden/make_fraw_fixtures.py; the bytes and headers are PDL's)
+GOLDEN = __import__("pathlib").Path(__file__).resolve().parent / "golden" / "fraw"
+F32_BAD = np.float32(-3.4028234663852886e38)
+
+
+def pdl_written():
+    """name -> (type, PDL dims, the values PDL wrote, header file or None)"""
+    fb = (np.arange(12, dtype=np.float32) / 4).reshape(2, 6)
+    fb[0, 1] = F32_BAD
+    fb[1, 4] = F32_BAD
+    return {
+        "seq_double": ("double", (5, 4, 3), np.arange(60, dtype=np.float64).reshape(3, 4, 5) * 1.5 - 7, None),
+        "seq_long": ("long", (7, 2), (np.arange(14, dtype=np.int32) * -3).reshape(2, 7), None),
+        "seq_byte": ("byte", (9,), np.arange(9, dtype=np.uint8), None),
+        "float_bad": ("float", (6, 2), fb, None),
+        "own_header": ("double", (3, 2), np.arange(6, dtype=np.float64).reshape(2, 3), "own_header.h"),
+    }
+
+
+@pytest.mark.parametrize("name", sorted(pdl_written()))
+def test_reads_files_pdl_wrote(name):
+    t, dims, want, hdr = pdl_written()[name]
+    y = P.readfraw(str(GOLDEN / name), header=str(GOLDEN / hdr) if hdr else None)
+    assert y.type == t and y.dims == dims
+    assert y.numpy().tobytes() == want.tobytes()
+    m = P.mapfraw(str(GOLDEN / name), ReadOnly=True, Header=str(GOLDEN / hdr) if hdr else None)
+    assert m.type == t and m.dims == dims and m.numpy().tobytes() == want.tobytes()
+
+
+def test_our_writer_matches_pdls_bytes(tmp_path):
+    for name, (t, dims, want, hdr) in pdl_written().items():
+        if hdr:
+            continue
+        P.writefraw(P.pdl(want), str(tmp_path / name))
+        assert (tmp_path / name).read_bytes() == (GOLDEN / name).read_bytes()
+        assert (tmp_path / (name + ".hdr")).read_text() == (GOLDEN / (name + ".hdr")).read_text()
+
+
+def test_mapfraw_creat_trunc_and_readonly(tmp_path):
+    name = str(tmp_path / "m")
+    x = P.mapfraw(name, Dims=[4, 3], Datatype=4, Creat=True)   # long->enum
+    assert (tmp_path / "m").stat().st_size == 4 * 3 * 4
+    assert (tmp_path / "m.hdr").read_text() == "4\n2\n4 3\n"        # long = 4 in PDL's order
+    assert x.type == "long" and np.all(x.numpy() == 0)
+    # the map is the file: bytes written to the file show through
+    with open(name, "r+b") as f:
+        f.write(np.arange(12, dtype=np.int32).tobytes())
+    assert np.array_equal(x.numpy().reshape(-1), np.arange(12))
+    # a header-described map; Trunc zero-fills
+    y = P.mapfraw(name, Trunc=True)
+    assert y.dims == (4, 3) and np.all(y.numpy() == 0)
+    # Datatype defaults to double
+    z = P.mapfraw(str(tmp_path / "d"), Dims=[5], Creat=True)
+    assert z.type == "double" and (tmp_path / "d").stat().st_size == 40
+    # read-only: refused as an op's output, as PDL refuses a read-only output
+    r = P.mapfraw(name, ReadOnly=True)
+    with pytest.raises(P.PDLError, match=r"PDL::Ufunc::sumover error: output parameter b is read-only"):
+        P.sumover(P.pdl(np.ones((3, 4, 5), np.int32)), out=r)
+    with pytest.raises(P.PDLError, match="opening file"):
+        P.mapfraw(str(tmp_path / "missing"), Dims=[2], ReadOnly=True)
+    with pytest.raises(P.PDLError, match="needs 80"):
+        P.mapfraw(str(tmp_path / "d"), Dims=[10])

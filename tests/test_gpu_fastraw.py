@@ -49,3 +49,26 @@ def test_view_written_contiguously(gpu, tmp_path):
     P.writefraw(v, name)
     y = P.readfraw(name)
     assert y.dims == v.dims and np.array_equal(y.numpy(), v.numpy())
+
+
+@pytest.mark.parametrize("name", ["seq_double", "seq_long", "seq_byte", "float_bad", "own_header"])
+def test_device_read_of_files_pdl_wrote(gpu, name):
+    """Files written by the reference PDL's writefraw, read into device memory."""
+    from test_fastraw import GOLDEN, pdl_written
+    t, dims, want, hdr = pdl_written()[name]
+    y = P.readfraw(str(GOLDEN / name), header=str(GOLDEN / hdr) if hdr else None, device=True)
+    assert y.on_device and y.type == t and y.dims == dims
+    assert y.numpy().tobytes() == want.tobytes()
+
+
+def test_mapfraw_device_results_reach_the_file(gpu, tmp_path):
+    """An op's output on the device, brought back to the host, is in the file."""
+    from test_fastraw import GOLDEN
+    src = P.mapfraw(str(GOLDEN / "seq_double"), ReadOnly=True).to_device()
+    name = str(tmp_path / "sums")
+    out = P.mapfraw(name, Dims=[4, 3], Creat=True)
+    P.sumover(src, out=out)
+    out.to_host()
+    want = (np.arange(60, dtype=np.float64).reshape(3, 4, 5) * 1.5 - 7).sum(-1)
+    assert np.fromfile(name, dtype=np.float64).tobytes() == want.tobytes()
+    assert P.readfraw(name).numpy().tobytes() == want.tobytes()
