@@ -219,9 +219,10 @@ pdlgb300_error pdlgb300_run_qsortveci(pdlgb300_ndarray *a, pdlgb300_ndarray *ind
  * unless `header` names one) holds "<type id>\n<ndims>\n<dim0> <dim1> ...\n".
  *   pdlgb300_fraw_header  -- shape and type x from the header (_read_frawhdr)
  *   pdlgb300_readfraw_into -- the file's bytes into x's memory: host `data`,
- *     or device `ddata` streamed through pinned staging buffers with the
- *     disk reads overlapping the copies (readfraw, without a pageable host
- *     copy); a short file leaves the rest zero, as readfraw's zeroes() does
+ *     or device `ddata` copied from a mapping of the file (a file that
+ *     cannot be mapped, a pipe for one, streams through pinned staging
+ *     buffers with the reads overlapping the copies); a short file leaves
+ *     the rest zero, as readfraw's zeroes() does
  *   pdlgb300_writefraw    -- header and data of a contiguous x (writefraw)
  * Device-memory transfers of one device share its two pinned staging
  * buffers: concurrent calls from several host threads are safe but take

@@ -5,10 +5,17 @@
 // memory (dim 0 fastest) and an ASCII header, by default "<name>.hdr":
 //   <type id>\n<ndims>\n<dim0> <dim1> ...\n
 // (_read_frawhdr / _writefrawhdr, FastRaw.pm:202-230).  A device-resident
-// read streams the file through two pinned staging buffers: while one
-// buffer's bytes are copied to the device, the next chunk of the file is
-// read into the other, so the data never lands in a pageable host copy.
+// read maps the file and copies the mapping to the device in 64 MiB pieces
+// (the driver streams mapped pages through its own staging; no copy of the
+// file is made in process memory).  Where the file cannot be mapped it is
+// streamed through two pinned staging buffers instead: while one buffer's
+// bytes are copied to the device, the next chunk is read into the other.
 #include "args.cuh"
+
+#include <fcntl.h>
+#include <sys/mman.h>
+#include <sys/stat.h>
+#include <unistd.h>
 
 #include <cerrno>
 #include <cstdio>
@@ -21,7 +28,7 @@
 namespace pg {
 namespace {
 
-constexpr size_t FRAW_CHUNK = (size_t)32 << 20;
+constexpr size_t FRAW_CHUNK = (size_t)32 << 20, FRAW_MAP_PIECE = (size_t)64 << 20;
 // element sizes in PDL's type order (sbyte .. double)
 constexpr size_t FSIZE[] = {1, 1, 2, 2, 4, 4, 8, 8, 8, 4, 8};
 
@@ -153,6 +160,31 @@ pdlgb300_error pdlgb300_readfraw_into(const char *name, pdlgb300_ndarray *x) {
     if (!e.error && got < len) memset(dst + got, 0, len - got);
     fclose(f);
     return e;
+  }
+  {
+    // the mapped file, copied in pieces
+    struct stat st;
+    const int fd = fileno(f);
+    if (fstat(fd, &st) == 0 && st.st_size > 0 && len > 0) {
+      const size_t avail = std::min(len, (size_t)st.st_size);
+      void *map = mmap(nullptr, avail, PROT_READ, MAP_PRIVATE, fd, 0);
+      if (map != MAP_FAILED) {
+        madvise(map, avail, MADV_SEQUENTIAL);
+        char *dst = (char *)x->ddata;
+        cudaError_t ce = cudaSuccess;
+        for (size_t off = 0; off < avail && ce == cudaSuccess; off += FRAW_MAP_PIECE)
+          ce = cudaMemcpyAsync(dst + off, (const char *)map + off,
+                               std::min(FRAW_MAP_PIECE, avail - off), cudaMemcpyHostToDevice,
+                               pgh::stream());
+        if (ce == cudaSuccess && avail < len)
+          ce = cudaMemsetAsync(dst + avail, 0, len - avail, pgh::stream());
+        if (ce == cudaSuccess) ce = cudaStreamSynchronize(pgh::stream());
+        munmap(map, avail);
+        fclose(f);
+        if (ce != cudaSuccess) return pgh::err(PDLGB300_EFATAL, "readfraw: %s", cudaGetErrorString(ce));
+        return pgh::ok();
+      }
+    }
   }
   Staging *s = nullptr;
   e = staging(&s);

@@ -1,8 +1,9 @@
 """PDL::IO::FastRaw (lib/PDL/IO/FastRaw.pm:198-350): an ndarray's bytes in
 one file and a text header beside it ("<name>.hdr" unless `header` names
-another file: type id, ndims, dims).  readfraw(device=True) streams the
-file into device memory through pinned staging buffers (the disk reads
-overlap the copies), so the data is never held in a pageable host copy."""
+another file: type id, ndims, dims).  readfraw(device=True) copies the
+file into device memory from a mapping of it (a file that cannot be mapped
+streams through pinned staging buffers, the reads overlapping the copies),
+so no copy of the data is made in process memory."""
 from __future__ import annotations
 
 import ctypes as C

@@ -72,3 +72,22 @@ def test_mapfraw_device_results_reach_the_file(gpu, tmp_path):
     want = (np.arange(60, dtype=np.float64).reshape(3, 4, 5) * 1.5 - 7).sum(-1)
     assert np.fromfile(name, dtype=np.float64).tobytes() == want.tobytes()
     assert P.readfraw(name).numpy().tobytes() == want.tobytes()
+
+
+def test_device_read_from_a_pipe_streams_through_staging(gpu, tmp_path):
+    """A FastRaw 'file' that cannot be mapped (a named pipe) goes through the
+    pinned staging buffers: several 32 MiB chunks and a short tail."""
+    import os
+    import threading
+    n = (80 << 20) // 8 + 123                       # 2.5 staging chunks of float64
+    a = np.arange(n, dtype=np.float64) * 0.5 - 7
+    name = str(tmp_path / "pipe")
+    os.mkfifo(name)
+    with open(name + ".hdr", "w") as f:
+        f.write(f"10\n1\n{n + 1000}\n")               # 1000 more than the pipe holds
+    w = threading.Thread(target=lambda: open(name, "wb").write(a.tobytes()), daemon=True)
+    w.start()
+    y = P.readfraw(name, device=True)
+    w.join(timeout=60)
+    got = y.numpy()
+    assert got[:n].tobytes() == a.tobytes() and np.all(got[n:] == 0)
