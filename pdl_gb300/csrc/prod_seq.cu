@@ -28,11 +28,8 @@
 //  3. Sequential continuation.  Rows whose products may leave the normal
 //     range run the reference's loop on from the prefix, one lane each.
 //
-// The float64 chain runs on the integer pipe (nmul) over chunks whose
-// partial products provably stay normal, and on the FP64 pipe (__dmul_rn)
-// elsewhere: the chain is latency-bound, and nmul's dependent steps are
-// shorter than the FP64 multiply's latency on GB300.
-#include "prod_int.cuh"
+// The float64 products use the FP64 pipe (__dmul_rn): the dependent chain
+// is latency-bound and the hardware multiply has the shortest latency.
 #include "reduce.cuh"
 
 namespace pg {
@@ -198,56 +195,6 @@ __global__ void __launch_bounds__(32) k_prod_seq(const RedArgs args, int64_t S) 
       // zero stops the reference's loop; later products of a zero are zero
       // or NaN, so only a chunk that ends zero or NaN is run again from its
       // start, element by element, to stop at the first zero.
-      bool done = false;
-      if constexpr (sizeof(Out) == 8) {
-        // The integer-pipe chain, where every partial product of the chunk
-        // provably stays normal: tmp and the chunk's elements normal, and
-        // the exponent after step k within [E + sum of negative element
-        // exponents, E + sum of positive ones + 2k] (a product's exponent
-        // is the sum of its operands' plus 0, 1 or 2) inside [-1021, 1022].
-        auto val = [&](int j, int &good) {
-          const In v = tile[st][j][lane];
-          good = !bad_el<In, BAD>(v, bv);
-          return good ? (Out)v : (Out)1;  // a bad element multiplies by 1
-        };
-        const uint64_t tb = (uint64_t)__double_as_longlong(tmp);
-        int E = (int)((hi_b32(tb) >> 20) & 0x7FFu);
-        bool ok = E != 0 && E != 0x7FF;
-        E -= 1023;
-        int lo_s = 0, hi_s = 0, ngood = 0;
-        for (int j = 0; j < m; j++) {
-          int good;
-          const uint32_t xh = hi_b32((uint64_t)__double_as_longlong(val(j, good)));
-          const int xe = (int)((xh >> 20) & 0x7FFu);
-          ok = ok && xe != 0 && xe != 0x7FF;
-          lo_s += min(xe - 1023, 0);
-          hi_s += max(xe - 1023, 0);
-          ngood += good;
-        }
-        ok = ok && E + lo_s >= -1021 && E + hi_s + 2 * m <= 1022;
-        if (ok) {
-          uint64_t A = (tb << 11) | (1ull << 63);
-          uint32_t S = hi_b32(tb) >> 31;
-          auto step = [&](int j) {
-            int good;
-            const uint64_t xb = (uint64_t)__double_as_longlong(val(j, good));
-            const uint32_t xh = hi_b32(xb);
-            S ^= xh >> 31;
-            nmul(A, E, (xb << 11) | (1ull << 63), (int)((xh >> 20) & 0x7FFu) - 1023);
-          };
-          if (m == PS_CH) {
-#pragma unroll 16
-            for (int j = 0; j < PS_CH; j++) step(j);
-          } else {
-            for (int j = 0; j < m; j++) step(j);
-          }
-          const uint64_t rb = ((uint64_t)S << 63) | ((uint64_t)(E + 1023) << 52) |
-                              ((A >> 11) & ((1ull << 52) - 1));
-          tmp = (Out)__longlong_as_double((long long)rb);
-          cnt += BAD ? ngood : m;
-          done = true;
-        }
-      }
       const Out start = tmp;
       auto elem = [&](int j) {
         const In v = tile[st][j][lane];
@@ -259,7 +206,6 @@ __global__ void __launch_bounds__(32) k_prod_seq(const RedArgs args, int64_t S) 
         }
         return x;
       };
-      if (!done) {
       if (m == PS_CH) {
 #pragma unroll
         for (int j = 0; j < PS_CH; j++) tmp = mul_rn(tmp, elem(j));
@@ -267,8 +213,7 @@ __global__ void __launch_bounds__(32) k_prod_seq(const RedArgs args, int64_t S) 
         for (int j = 0; j < m; j++) tmp = mul_rn(tmp, elem(j));
       }
       if constexpr (!BAD) cnt += m;
-      }
-      if (!done && (is_zero_bits(tmp) || tmp != tmp)) {
+      if (is_zero_bits(tmp) || tmp != tmp) {
         tmp = start;
         for (int j = 0; j < m; j++) {
           const In v = tile[st][j][lane];
