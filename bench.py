@@ -812,6 +812,18 @@ def bench_sort(args, P, torch, stream, hbm):
                           "sample": "8192 of the 65536 rows"}
     out["bound"] = ("a warp per row: bitonic network in shared memory (the reference's "
                     "quicksort on the rows whose result could depend on the sort)")
+    # longer rows: a block per row (float32 dims (2048, 4096), N(0,1), seed 12)
+    al = np.random.default_rng(12).standard_normal((4096, 2048), dtype=np.float32)
+    xl = P.pdl(al).to_device()
+    r = P.medover(xl)
+    P.sync()
+    ms = time_op(torch, stream, lambda: P.medover(xl), 5)
+    want = O.run("medover", [P.pdl(np.ascontiguousarray(al[:256]))], nthreads=n)[0].numpy()
+    out["medover_rows_of_2048"] = {
+        "config": "medover, float32 dims (2048, 4096) N(0,1) seed 12: 4096 rows of 2048",
+        "ms": ms, "rows_per_s": 4096 / (ms * 1e-3), "gbs_in": al.nbytes / (ms * 1e-3) / 1e9,
+        "kernel": "k_sortred_block", "error_vs_oracle": errs(r.numpy()[:256], want)}
+    del r, xl
     # vector sorts: 512 planes of 2048 points in 3-D (float64, N(0,1), seed 11)
     v = np.random.default_rng(11).standard_normal((512, 2048, 3))
     xv = P.pdl(v).to_device()

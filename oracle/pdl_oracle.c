@@ -1407,6 +1407,12 @@ int oracle_npdls(const char *opname) {
   return op < 0 ? -1 : OPS[op].npdls;
 }
 
+/* Number of input ndarrays of an op, -1 if unknown. */
+int oracle_nparents(const char *opname) {
+  int op = find_op(opname);
+  return op < 0 ? -1 : OPS[op].nparents;
+}
+
 /* Name of an op's parameter j (the pp_def signature's), or NULL. */
 const char *oracle_par_name(const char *opname, int j) {
   int op = find_op(opname);

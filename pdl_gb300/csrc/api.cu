@@ -1229,11 +1229,13 @@ pdlgb300_error dispatch_sortred(RunCtx &c, int kind) {
     return err(PDLGB300_EUSERERROR, "Error in %s:cannot process empty ndarray", c.vt->name);
   if (g.rows == 0 || g.n == 0) return ok();
   void *scratch = nullptr;
-  const size_t vbytes = ((size_t)g.rows * g.n * TSIZES[dt] + 15) & ~(size_t)15;
-  const size_t ibytes = kind == SR_QSORTI ? (size_t)g.rows * g.n * sizeof(int64_t) : 0;
-  RET_IF(dalloc(vbytes + ibytes, &scratch));
-  g.scratch = scratch;
-  g.iscratch = ibytes ? (int64_t *)((char *)scratch + vbytes) : nullptr;
+  if (g.n > SORT_SHARED_MAXN) {  // (shorter rows sort in shared memory)
+    const size_t vbytes = ((size_t)g.rows * g.n * TSIZES[dt] + 15) & ~(size_t)15;
+    const size_t ibytes = kind == SR_QSORTI ? (size_t)g.rows * g.n * sizeof(int64_t) : 0;
+    RET_IF(dalloc(vbytes + ibytes, &scratch));
+    g.scratch = scratch;
+    g.iscratch = ibytes ? (int64_t *)((char *)scratch + vbytes) : nullptr;
+  }
   int *w = nullptr;
   pdlgb300_error e = status_word(&w);
   g.err = w;
@@ -1248,7 +1250,7 @@ pdlgb300_error dispatch_sortred(RunCtx &c, int kind) {
     if (ce == cudaSuccess) ce = cudaStreamSynchronize(g_stream);
     if (ce != cudaSuccess) e = err(PDLGB300_EFATAL, "%s: %s", c.vt->name, cudaGetErrorString(ce));
   }
-  cudaFreeAsync(scratch, g_stream);
+  if (scratch) cudaFreeAsync(scratch, g_stream);
   if (!e.error && hs) e = err(PDLGB300_EFATAL, "%s: a sort scan left its range", c.vt->name);
   return e;
 }

@@ -140,6 +140,9 @@ struct SortArgs {
   int *err;           // bit 0: a scan left its range (never expected)
 };
 pdlgb300_error launch_sortred(int kind, int dt, const SortArgs &g, cudaStream_t s);
+// rows up to this length sort in shared memory (warp or block kernels); the
+// scratch copies serve longer rows only
+constexpr int64_t SORT_SHARED_MAXN = 8192;
 
 // qsortvec / qsortveci: a(n,m) -> b(n,m) or indx(m)
 struct VecSortArgs {

@@ -40,8 +40,9 @@ constexpr uint32_t TMEM_COLS = 512;  // two 256-column slab accumulators
 constexpr long long WAIT_CYCLES = 8000000000LL;  // ~4 s at 2 GHz
 
 // K-slabs accumulated in one TMEM buffer before the accumulator warps
-// drain it into round-to-nearest registers
-constexpr int SPB = 1;
+// drain it into round-to-nearest registers (2: 64-deep chains, 24
+// truncating accumulations for bf16x6; the drain runs half as often)
+constexpr int SPB = 2;
 
 template <int LIMBS> struct TcCfg {
   static constexpr int STAGES = LIMBS == 3 ? 3 : 4;

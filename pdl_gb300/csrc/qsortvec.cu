@@ -272,7 +272,8 @@ pdlgb300_error go(const VecSortArgs &g, size_t smem_limit, cudaStream_t s) {
   const size_t smem = qsortvec_smem_bytes(g.n, g.m, (int)sizeof(T));
   if (g.m < (1 << 30) && smem <= smem_limit) {
     auto kern = k_qsortvec_block<T, IND, BAD>;
-    if (smem > 48 * 1024 &&
+    // (the kernel's own static shared words count against the default 48 KB too)
+    if (smem + 1024 > 48 * 1024 &&
         !pgh::cuda_check(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                               (int)smem), &e, "qsortvec smem"))
       return e;

@@ -379,6 +379,169 @@ __global__ void __launch_bounds__(SF_WARPS * 32) k_sortred_warp(const SortArgs g
   }
 }
 
+// Longer rows (SF_MAX < n <= SB_MAX): one block per row over dynamic
+// shared memory, the warp kernel's steps at block scale: good values
+// compacted in order (block-wide, from per-warp ballots), the bitonic
+// network where the result cannot depend on the sort, else the reference's
+// quicksort by thread 0 over the same copy.
+constexpr int SB_MAX = 8192, SB_THREADS = 256;
+
+template <class T, int K, bool BAD>
+__global__ void __launch_bounds__(SB_THREADS) k_sortred_block(const SortArgs g) {
+  constexpr bool IND = K == SR_QSORTI;
+  extern __shared__ __align__(16) unsigned char sb_smem[];
+  const int n = (int)g.n;
+  int Pmax = 1;
+  while (Pmax < n) Pmax <<= 1;
+  T *const v = reinterpret_cast<T *>(sb_smem);
+  int32_t *const ix = reinterpret_cast<int32_t *>(sb_smem + (size_t)Pmax * sizeof(T));
+  __shared__ int s_cnt[SB_THREADS / 32], s_fl;
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  const unsigned lt = (1u << lane) - 1u;
+  const Bad<T> bv{from_bits<T>(g.abad), (bool)g.abad_isnan};
+  const T obad = from_bits<T>(g.obad);
+  // block-wide counts of the warps before this one, and the totals
+  auto scan2 = [&](unsigned gm, unsigned bm, int &gb, int &bb, int &gt, int &bt) {
+    if (lane == 0) s_cnt[w] = (__popc(gm) << 16) | __popc(bm);
+    __syncthreads();
+    gb = bb = gt = bt = 0;
+    for (int k = 0; k < SB_THREADS / 32; k++) {
+      const int c = s_cnt[k];
+      if (k < w) {
+        gb += c >> 16;
+        bb += c & 0xFFFF;
+      }
+      gt += c >> 16;
+      bt += c & 0xFFFF;
+    }
+    __syncthreads();  // s_cnt is reused by the next call
+  };
+  for (int64_t row = blockIdx.x; row < g.rows; row += gridDim.x) {
+    int64_t offs[MAXP];
+    loop_offsets(g.L, row, offs);
+    const T *a = reinterpret_cast<const T *>(g.a) + offs[0];
+    if (tid == 0) s_fl = 0;
+    int nn = 0, nbad = 0;
+    bool unsafe = false, neg0 = false, pos0 = false;
+    for (int base = 0; base < n; base += SB_THREADS) {
+      const int t = base + tid;
+      T x = (T)0;
+      bool good = false;
+      if (t < n) {
+        x = a[(int64_t)t * g.inc_a];
+        good = !(K != SR_MODE && BAD && bv.is(x));
+      }
+      const unsigned gm = __ballot_sync(0xffffffffu, good);
+      const unsigned bm = __ballot_sync(0xffffffffu, t < n && !good);
+      int gb, bb, gt, bt;
+      scan2(gm, bm, gb, bb, gt, bt);
+      if (good) {
+        const int pos = nn + gb + __popc(gm & lt);
+        if constexpr (IND) ix[pos] = t;
+        else v[pos] = x;
+        unsafe |= sf_unsafe_float<T>(x, neg0, pos0);
+      }
+      if constexpr (IND) {
+        if (t < n) v[t] = x;
+        if (t < n && !good)
+          reinterpret_cast<int64_t *>(g.b)[offs[g.out_pdl] +
+                                           (int64_t)(n - 1 - (nbad + bb + __popc(bm & lt))) * g.inc_b] = t;
+      }
+      nn += gt;
+      nbad += bt;
+    }
+    if (unsafe) atomicOr(&s_fl, 1);
+    if (neg0) atomicOr(&s_fl, 2);
+    if (pos0) atomicOr(&s_fl, 4);
+    __syncthreads();
+    unsafe = (s_fl & 1) || (s_fl & 6) == 6;
+    int P = 1;
+    while (P < nn) P <<= 1;
+    if (!unsafe && nn > 1) {
+      if constexpr (!IND) {
+        for (int i = nn + tid; i < P; i += SB_THREADS) v[i] = (T)0;
+        for (int i = tid; i < P; i += SB_THREADS) ix[i] = i;  // tie-break by position
+      } else {
+        for (int i = nn + tid; i < P; i += SB_THREADS) ix[i] = -1;
+      }
+      __syncthreads();
+      for (int k = 2; k <= P; k <<= 1) {
+        for (int j = k >> 1; j > 0; j >>= 1) {
+          for (int i = tid; i < P; i += SB_THREADS) {
+            const int l = i ^ j;
+            if (l > i) {
+              bool greater;  // element i after element l
+              const int32_t pi = ix[i], pl = ix[l];
+              if constexpr (IND) {
+                if (pi < 0) greater = pl >= 0;
+                else if (pl < 0) greater = false;
+                else greater = v[pl] < v[pi] || (v[pl] == v[pi] && pl < pi);
+              } else {
+                const bool si = pi >= nn, sl = pl >= nn;
+                if (si || sl) greater = si && (!sl || pl < pi);
+                else greater = v[l] < v[i] || (v[l] == v[i] && pl < pi);
+              }
+              if (greater == ((i & k) == 0)) {
+                if constexpr (!IND) {
+                  const T tv = v[i];
+                  v[i] = v[l];
+                  v[l] = tv;
+                }
+                ix[i] = pl;
+                ix[l] = pi;
+              }
+            }
+          }
+          __syncthreads();
+        }
+      }
+      if constexpr (IND) {
+        // equal values: the reference's order of their indices is its own
+        bool tie = false;
+        for (int i = tid; i + 1 < nn; i += SB_THREADS) tie |= v[ix[i]] == v[ix[i + 1]];
+        if (tie) atomicOr(&s_fl, 8);
+        __syncthreads();
+        if (s_fl & 8) {
+          unsafe = true;
+          int m = 0;  // the good positions in order again
+          for (int base = 0; base < n; base += SB_THREADS) {
+            const int t = base + tid;
+            const bool good = t < n && !(BAD && bv.is(v[t]));
+            const unsigned gm = __ballot_sync(0xffffffffu, good);
+            int gb, bb, gt, bt;
+            scan2(gm, 0u, gb, bb, gt, bt);
+            if (good) ix[m + gb + __popc(gm & lt)] = t;
+            m += gt;
+          }
+        }
+      }
+    }
+    __syncthreads();
+    if (unsafe && nn > 1 && tid == 0) {
+      bool ok;
+      if constexpr (IND) ok = qs_indices<T, int32_t>(v, ix, 0, nn - 1);
+      else ok = qs_values<T>(v, 0, nn - 1);
+      if (!ok) atomicOr(g.err, 1);
+    }
+    __syncthreads();
+    if constexpr (IND) {
+      int64_t *out = reinterpret_cast<int64_t *>(g.b) + offs[g.out_pdl];
+      for (int i = tid; i < nn; i += SB_THREADS) out[(int64_t)i * g.inc_b] = ix[i];
+    } else {
+      T *out = reinterpret_cast<T *>(g.b) + offs[g.out_pdl];
+      finish_values<T, K>(g, v, nn, offs, out, obad, tid, SB_THREADS);
+    }
+    __syncthreads();
+  }
+}
+
+// dynamic shared memory of k_sortred_block for rows of n values of tsize bytes
+size_t sortred_block_smem(int64_t n, int tsize) {
+  int64_t P = 1;
+  while (P < n) P <<= 1;
+  return (size_t)P * (tsize + 4);
+}
+
 template <class T, int K>
 pdlgb300_error go_sort(const SortArgs &g, cudaStream_t s) {
   pdlgb300_error e = pgh::ok();
@@ -392,6 +555,21 @@ pdlgb300_error go_sort(const SortArgs &g, cudaStream_t s) {
     pgh::record_kernel("k_sortred_warp", grid, SF_WARPS * 32);
     return e;
   }
+  if (g.n <= SB_MAX) {
+    const size_t smem = sortred_block_smem(g.n, (int)sizeof(T));
+    auto kern = g.bad ? k_sortred_block<T, K, true> : k_sortred_block<T, K, false>;
+    // (the kernel's own static shared words count against the default 48 KB too)
+    if (smem + 1024 > 48 * 1024 &&
+        !pgh::cuda_check(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)smem), &e, "k_sortred_block smem"))
+      return e;
+    const int64_t grid = std::max<int64_t>(1, std::min<int64_t>(g.rows, (int64_t)nsm * 8));
+    kern<<<(int)grid, SB_THREADS, smem, s>>>(g);
+    if (!pgh::cuda_check(cudaGetLastError(), &e, "k_sortred_block")) return e;
+    pgh::record_kernel("k_sortred_block", grid, SB_THREADS);
+    return e;
+  }
+  if (!g.scratch) return pgh::err(PDLGB300_EFATAL, "sort: no scratch for long rows");
   const int64_t grid = std::max<int64_t>(1, std::min<int64_t>((g.rows + 127) / 128, (int64_t)nsm * 16));
   if (g.bad) k_sortred<T, K, true><<<(int)grid, 128, 0, s>>>(g);
   else k_sortred<T, K, false><<<(int)grid, 128, 0, s>>>(g);

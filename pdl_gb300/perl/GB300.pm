@@ -23,15 +23,28 @@ bootstrap PDL::GB300 $VERSION;
 
 our %saved;    # PDL's own subs, kept by install()
 
-# a(n); [o]b() reductions over dim 0
+# a(n); [o]b() reductions over dim 0, and the one-input sort-based functions
+# (a(n) or a(n,m) in, one output)
 our @REDUCE = qw(sumover dsumover prodover dprodover average daverage minimum maximum
                  minimum_ind maximum_ind cumusumover dcumusumover cumuprodover dcumuprodover
-                 andover orover xorover zcover bandover borover bxorover firstnonzeroover);
+                 andover orover xorover zcover bandover borover bxorover firstnonzeroover
+                 qsort qsorti medover oddmedover modeover qsortvec qsortveci);
+# Inplace => 1 among them (lib/PDL/Ufunc.pd:1042,1117)
+my %INPLACE = map { $_ => 1 } qw(qsort qsortvec);
+# a(n); p(); [o]b()
+our @PCT = qw(pctover oddpctover);
 # a(); b(); [o]c(); OtherPars swap
 our @BIOP = qw(plus mult minus divide gt lt le ge eq ne shiftleft shiftright or2 and2 xor);
 my %CMP = map { $_ => 1 } qw(gt lt le ge eq ne);    # Comparison ops (Ops.pd:297-302)
 
 sub _is_pdl { UNIVERSAL::isa($_[0], 'PDL') }
+
+# More arguments than the signature has fail as the generated XS fails
+# ("Usage: PDL::op(a, b=b)").
+sub _usage {
+  my ($op, $sig, $max, @args) = @_;
+  PDL::Core::barf("Usage: PDL::$op($sig)") if @args > $max;
+}
 
 # A new output, made as PDL::PP's XS makes one (PDL_XS_PREAMBLE and
 # PDL_XS_pdlinit, lib/PDL/Core/pdlperl.h:4-45): in the class of the first
@@ -62,11 +75,39 @@ for my $op (@REDUCE) {
   no strict 'refs';
   *{"PDL::GB300::$op"} = sub {
     if (my $f = _pdl_op($op, \@_)) { return $f->(@_) }
+    _usage($op, 'a, b=b', 2, @_);
     my ($a, $b) = @_;
-    $b = _new_out($a) unless _is_pdl($b);
+    if ($INPLACE{$op} && _is_pdl($a) && $a->is_inplace) {
+      PDL::Core::barf("inplace input but different output given") if defined $b;
+      $b = $a;
+      $a->set_inplace(0);
+    }
+    $b = _new_out($a) unless defined $b;
     _run($op, [$a, $b], 0);
     return $b;
   };
+}
+
+for my $op (@PCT) {
+  no strict 'refs';
+  *{"PDL::GB300::$op"} = sub {
+    if (my $f = _pdl_op($op, \@_)) { return $f->(@_) }
+    _usage($op, 'a, p, b=b', 3, @_);
+    my ($a, $p, $b) = @_;
+    $b = _new_out($a) unless defined $b;
+    _run($op, [$a, $p, $b], 0);
+    return $b;
+  };
+}
+
+# a(n); [o]cmin(); [o]cmax(); indx [o]cmin_ind(); indx [o]cmax_ind()
+sub minmaximum {
+  if (my $f = _pdl_op('minmaximum', \@_)) { return $f->(@_) }
+  _usage('minmaximum', 'a, cmin=cmin, cmax=cmax, cmin_ind=cmin_ind, cmax_ind=cmax_ind', 5, @_);
+  my ($a, @o) = @_;
+  $o[$_] = _new_out($a) for grep { !defined $o[$_] } 0 .. 3;
+  _run('minmaximum', [$a, @o], 0);
+  return @o;
 }
 
 # Called as op($a, $b), op($a, $b, $swap) (the operator overloads),
@@ -76,6 +117,7 @@ for my $op (@BIOP) {
   no strict 'refs';
   *{"PDL::GB300::$op"} = sub {
     if (my $f = _pdl_op($op, \@_)) { return $f->(@_) }
+    _usage($op, 'a, b, c=c, swap=swap', 4, @_);
     my ($a, $b, @rest) = @_;
     my ($c, $swap);
     if (@rest == 1 && !_is_pdl($rest[0])) { $swap = $rest[0] }
@@ -85,7 +127,7 @@ for my $op (@BIOP) {
       $c = $a;
       $a->set_inplace(0);
     }
-    $c = _new_out($_[0]) unless _is_pdl($c);
+    $c = _new_out($_[0]) unless defined $c;
     _badval_warn($a, $b, $swap ? 1 : 0) if $CMP{$op};
     _run($op, [$a, $b, $c], $swap ? 1 : 0);
     return $c;
@@ -94,8 +136,9 @@ for my $op (@BIOP) {
 
 sub inner {
   if (my $f = _pdl_op('inner', \@_)) { return $f->(@_) }
+  _usage('inner', 'a, b, c=c', 3, @_);
   my ($a, $b, $c) = @_;
-  $c = _new_out($a) unless _is_pdl($c);
+  $c = _new_out($a) unless defined $c;
   _run('inner', [$a, $b, $c], 0);
   return $c;
 }
@@ -163,7 +206,7 @@ sub import {
 sub install {
   no strict 'refs';
   no warnings 'redefine';
-  for my $op (@REDUCE, @BIOP, qw(inner matmult)) {
+  for my $op (@REDUCE, @PCT, @BIOP, qw(inner matmult minmaximum)) {
     $saved{$op} //= \&{"PDL::$op"};
     *{"PDL::$op"} = \&{"PDL::GB300::$op"};
   }

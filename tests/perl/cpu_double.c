@@ -21,6 +21,7 @@ int oracle_run(const char *opname, pdlgb300_ndarray **pdls_in, const int64_t *ot
 
 const char *oracle_op_package(const char *name);
 const char *oracle_par_name(const char *opname, int j);
+int oracle_nparents(const char *opname);
 
 static char msg[4096];
 
@@ -65,7 +66,7 @@ const pdlgb300_vtable *pdlgb300_get_vtable(const char *name) {
   for (int j = 0; j < np; j++) names[j] = oracle_par_name(name, j);
   v->par_names = names;
   v->npdls = np;
-  v->nparents = np - 1; /* every op the module routes has one output */
+  v->nparents = oracle_nparents(name);
   return v;
 }
 

@@ -894,3 +894,29 @@ def test_sort_based_empty_and_errors(gpu):
     e = P.qsort(P.zeroes("double", 0))          # the reference returns at once
     assert e.dims == (0,)
     assert P.qsorti(P.pdl(np.array([8.0]))).numpy().tolist() == [0]
+
+
+@pytest.mark.parametrize("t", ["byte", "long", "float", "double"])
+@pytest.mark.parametrize("op", SORT_OPS + ["pctover", "modeover"])
+def test_sort_based_long_rows(gpu, op, t):
+    """Rows of 513 to 8192 elements (a block per row in shared memory) and
+    beyond (one thread per row): ties, NaN and signed zeros, distinct
+    values (the network), bad values."""
+    if op == "modeover" and t in ("float", "double"):
+        return
+    rng = seeded(("sortlong", op, t))
+    for n in [513, 1000, 2048, 5000, 8192, 9000]:
+        datas = [_sort_data(rng, t, (3, n))]
+        if t in ("float", "double", "long"):
+            datas.append(rng.permutation(np.arange(3 * n)).reshape(3, n).astype(NP_DTYPES[type_code(t)]))
+        for a in datas:
+            x = to_pdl(a, t)
+            ins = [x, P.pdl(np.array(0.37))] if op == "pctover" else [x]
+            got, exp = _run_both(op, ins)
+            _bits_equal(got, exp, f"{op} {t} n={n}")
+    if op != "modeover":
+        a = _sort_data(rng, t, (4, 3000), bad_frac=0.2)
+        x = to_pdl(a, t, badflag=True)
+        ins = [x, P.pdl(np.array(0.37))] if op == "pctover" else [x]
+        got, exp = _run_both(op, ins)
+        _bits_equal(got, exp, f"{op} {t} bad n=3000")

@@ -103,5 +103,6 @@ def test_reference_suite_through_the_glue(pdl_lib, glue_on_double, tmp_path):
         runs[op] = runs.get(op, 0) + int(n)
     # the path's ops went through the glue
     for op in ("sumover", "prodover", "average", "minimum", "maximum", "cumusumover", "plus",
-               "mult", "inner", "matmult"):
+               "mult", "inner", "matmult", "qsort", "qsorti", "qsortvec", "medover", "pctover",
+               "minmaximum"):
         assert runs.get(op, 0) > 0, (op, runs)
