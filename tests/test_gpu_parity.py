@@ -920,3 +920,30 @@ def test_sort_based_long_rows(gpu, op, t):
         ins = [x, P.pdl(np.array(0.37))] if op == "pctover" else [x]
         got, exp = _run_both(op, ins)
         _bits_equal(got, exp, f"{op} {t} bad n=3000")
+
+
+@pytest.mark.parametrize("where", ["host", "device"])
+def test_in_place_outputs(gpu, where):
+    """An output that is one of the inputs (PDL's Inplace => 1: the binary
+    ops, qsort, qsortvec), on host and device memory: the same values as a
+    separate output."""
+    rng = seeded(("inplace", where))
+    for op in ("plus", "mult", "minus", "divide"):
+        a, _ = rand_array(rng, "double", (5, 7), 1, 9)
+        b, _ = rand_array(rng, "double", (5, 7), 1, 9)
+        x, y = to_pdl(a, "double"), to_pdl(b, "double")
+        exp = O.run(op, [x, y])[0]
+        if where == "device":
+            x.to_device()
+            y.to_device()
+        got = getattr(P, op)(x, y, out=x)
+        assert got is x
+        assert_same(x, exp, what=f"{op} in place ({where})")
+    for op, shape in (("qsort", (9, 1000)), ("qsort", (3, 700)), ("qsortvec", (40, 3, 3))):
+        a = rng.standard_normal(shape)
+        x = to_pdl(a, "double")
+        exp = O.run(op, [x])[0]
+        if where == "device":
+            x.to_device()
+        got = getattr(P, op)(x, out=x)
+        _bits_equal(got, exp, f"{op} in place ({where}) {shape}")
