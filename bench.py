@@ -627,11 +627,11 @@ def bench_c2(args, P, torch, stream):
 
 
 def c4_inputs():
-    rng = np.random.default_rng(6)
-    X = (0.1 * rng.standard_normal((8192, 512))).astype(np.float32)   # PDL X(t=512, h=8192)
-    Wm = (0.1 * rng.standard_normal((512, 256))).astype(np.float32)   # PDL W(w=256, t=512)
-    bias = (0.1 * rng.standard_normal(256)).astype(np.float32)        # PDL bias(w=256)
-    return X, Wm, bias
+    """X PDL dims (t=512, h=8192), W (w=256, t=512), bias (w=256): the
+    seeded generator shared with the tests."""
+    import config_inputs as CI
+    d = CI.c4()
+    return d["X"], d["W"], d["bias"]
 
 
 def bench_c4(args, P, torch, stream):
@@ -688,6 +688,13 @@ def bench_c4(args, P, torch, stream):
     ref = {"X": gZ @ W64.T, "W": X64.T @ gZ, "bias": gZ.sum(0)}
     got = {"X": gX, "W": gW, "bias": gb}
     normwise = {k: float(np.max(np.abs(got[k] - ref[k])) / np.max(np.abs(ref[k]))) for k in ref}
+    fx = pdl_fixtures()
+    vs_pdl = None
+    if fx is not None and "c4/gbias" in fx.files:
+        # against dL/dX, dL/dW, dL/dbias written out by hand in PDL (float64)
+        pdl_g = {"X": (gX[::256], fx["c4/gX/sample"]), "W": (gW[::8], fx["c4/gW/sample"]),
+                 "bias": (gb, fx["c4/gbias"])}
+        vs_pdl = {k: errs(g, w) for k, (g, w) in pdl_g.items()}
     rng = np.random.default_rng(60)
     eps, fd_err = 1e-3, 0.0
 
@@ -717,6 +724,7 @@ def bench_c4(args, P, torch, stream):
             "bwd_tflops": bwd_flop / (ms_b * 1e-3) / 1e12,
             "max_rel_err_vs_fp64_central_fd_64_coords": fd_err,
             "max_normwise_err_vs_fp64_gradient": normwise,
+            "error_vs_gradient_by_hand_in_reference_pdl": vs_pdl,
             "kernels": "k_mm_tc_bf16x6 (matmult and its adjoints), k_biop, k_red_rows, k_unb_*"}
 
 

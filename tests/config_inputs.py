@@ -138,3 +138,13 @@ def c3_matmult(nb=16):
     a = rng.standard_normal((nb, 2048, 1024)).astype(np.float32)
     b = rng.standard_normal((1024, 2048)).astype(np.float32)
     return {"a": a, "b": b}
+
+
+def c4():
+    """The adjoint workload: X float32 PDL dims (512, 8192), W (256, 512),
+    bias (256), each 0.1 N(0, 1), seed 6 (numpy shapes reversed)."""
+    rng = np.random.default_rng(6)
+    X = (0.1 * rng.standard_normal((8192, 512))).astype(np.float32)
+    W = (0.1 * rng.standard_normal((512, 256))).astype(np.float32)
+    bias = (0.1 * rng.standard_normal(256)).astype(np.float32)
+    return {"X": X, "W": W, "bias": bias}

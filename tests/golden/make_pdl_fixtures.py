@@ -157,6 +157,27 @@ def main() -> int:
                        "sample": "batches [0, 11], rows (h) ::256, every w"}
         del x, r
 
+        # ---------------- the adjoint workload's gradients, by hand in PDL (FP64)
+        # L = sumover(sumover((X x W + bias)**2)) / 8192; G = dL/dZ = 2 Z / 8192
+        x = CI.c4()
+        for k in ("X", "W", "bias"):
+            write_fraw(d / f"c4{k}", x[k])
+        run_perl(pdl, f'my $X = readfraw("{d}/c4X")->double; my $W = readfraw("{d}/c4W")->double;\n'
+                      f'my $b = readfraw("{d}/c4bias")->double;\n'
+                      'my $G = 2 * (($X x $W) + $b) / 8192;\n'
+                      f'writefraw($G x $W->transpose, "{d}/c4_gX");\n'
+                      f'writefraw($X->transpose x $G, "{d}/c4_gW");\n'
+                      f'writefraw($G->xchg(0, 1)->sumover, "{d}/c4_gbias");\n')
+        gX, gW, gb = (read_fraw(d / f"c4_{k}") for k in ("gX", "gW", "gbias"))
+        fx["c4/gX/sample"] = np.ascontiguousarray(gX[::256])     # numpy (8192, 512): rows ::256
+        fx["c4/gW/sample"] = np.ascontiguousarray(gW[::8])       # numpy (512, 256): rows ::8
+        fx["c4/gbias"] = gb
+        meta["c4"] = {"input_sha256": [CI.sha(x[k]) for k in ("X", "W", "bias")],
+                      "sha256": {"gX": CI.sha(gX), "gW": CI.sha(gW), "gbias": CI.sha(gb)},
+                      "what": "dL/dX, dL/dW, dL/dbias by hand in PDL, float64",
+                      "sample": "gX numpy rows ::256, gW numpy rows ::8, gbias whole"}
+        del x, gX, gW, gb
+
     env = dict(os.environ, PERL5LIB=f"{pdl}/shims:{pdl}/src/blib/lib:{pdl}/src/blib/arch")
     ver = subprocess.run(["perl", "-MPDL", "-e",
                           'print "$PDL::VERSION ", PDL::Core::pthreads_enabled(), " ", '

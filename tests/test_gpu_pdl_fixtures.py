@@ -144,3 +144,27 @@ def test_c3_matmult_against_pdl(gpu):
         P.set_matmult_mode(P.MATMULT_BF16X6)
     assert np.array_equal(bits(exact), bits(want))                  # the reference's order
     assert np.all(np.abs(split.astype(np.float64) - want) <= (2 * 1024 + 8) * EPS32 * scale)
+
+
+def test_c4_adjoints_against_gradients_by_hand_in_pdl(gpu):
+    """The hand-written adjoint kernels (float32) on the adjoint workload
+    against dL/dX, dL/dW, dL/dbias written out by hand in PDL (float64):
+    normwise error (max |diff| / max |gradient|) within 2e-6."""
+    x = CI.c4()
+    assert [CI.sha(x[k]) for k in ("X", "W", "bias")] == META["c4"]["input_sha256"]
+    X, W, b = (P.pdl(x[k]).to_device() for k in ("X", "W", "bias"))
+    Y = P.matmult(X, W)
+    Z = P.plus(Y, b)
+    S = P.mult(Z, Z)
+    s1 = P.sumover(S)
+    gL = P.pdl(np.array(1.0 / 8192, np.float32)).to_device()
+    g_s1 = P.sumover_bwd(gL, s1)
+    g_S = P.sumover_bwd(g_s1, S)
+    gz1, gz2 = P.mult_bwd(g_S, Z, Z)
+    g_Y, g_b = P.plus_bwd(P.plus(gz1, gz2), Y, b)
+    g_X, g_W = P.matmult_bwd(g_Y, X, W)
+    got = {"gX": g_X.numpy()[::256], "gW": g_W.numpy()[::8], "gbias": g_b.numpy()}
+    for k, g in got.items():
+        want = FX[f"c4/{k}/sample"] if k != "gbias" else FX["c4/gbias"]
+        nw = np.max(np.abs(g.astype(np.float64) - want)) / np.max(np.abs(want))
+        assert nw <= 2e-6, (k, nw)

@@ -98,3 +98,16 @@ def test_c3_matmult_bit_for_bit_on_sampled_rows():
     a = np.ascontiguousarray(x["a"][[0, 11]][:, ::256, :])   # batches 0, 11; rows h ::256
     got = O.run("matmult", [P.pdl(a), P.pdl(x["b"])], nthreads=NTH)[0].numpy()
     assert np.array_equal(bits(got), bits(FX["c3m/sample"]))
+
+
+def test_c4_gradients_by_hand_in_pdl_are_the_fp64_gradients():
+    """The fixture's gradients (written out by hand in PDL, float64) equal
+    numpy's float64 evaluation of the same formulas to rounding."""
+    x = CI.c4()
+    assert [CI.sha(x[k]) for k in ("X", "W", "bias")] == META["c4"]["input_sha256"]
+    X, W, b = (x[k].astype(np.float64) for k in ("X", "W", "bias"))
+    G = 2.0 * (X @ W + b) / 8192.0
+    want = {"gX": (G @ W.T)[::256], "gW": (X.T @ G)[::8], "gbias": G.sum(0)}
+    for k, w in want.items():
+        got = FX[f"c4/{k}/sample"] if k != "gbias" else FX["c4/gbias"]
+        assert np.max(np.abs(got - w)) <= 1e-12 * np.max(np.abs(w)), k
