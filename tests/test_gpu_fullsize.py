@@ -169,3 +169,22 @@ def test_c3_inner_float64_full_size(gpu):
     want = np.einsum("ij,ij->i", a, b)
     scale = np.einsum("ij,ij->i", np.abs(a), np.abs(b))
     assert np.all(np.abs(got - want) <= (4096 + 2) * EPS64 * scale)
+
+
+def test_rows_beyond_2_31_elements(gpu):
+    """64-bit indexing: one row of 2^31 + 77 bytes (2 GiB) through a sum,
+    a max index past 2^31, a minimum, and an elementwise op over all of it."""
+    n = (1 << 31) + 77
+    a = np.zeros(n, np.uint8)
+    a[[5, 1 << 31, n - 1]] = [1, 2, 3]
+    x = P.pdl(a).to_device()
+    assert P.sumover(x).numpy() == 6
+    assert P.maximum_ind(x).numpy() == n - 1
+    a[n - 1] = 0
+    y = P.pdl(a).to_device()
+    assert P.maximum_ind(y).numpy() == 1 << 31
+    assert P.minimum(y).numpy() == 0
+    z = P.plus(y, y)                                  # byte + byte, 2^31 + 77 outputs
+    zs = P.sumover(z).numpy()
+    assert zs == 2 * (1 + 2)
+    del x, y, z
