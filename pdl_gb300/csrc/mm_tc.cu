@@ -58,6 +58,7 @@ struct TcArgs {
   int64_t nA, nB;  // limb batches (1 when the operand is broadcast)
   Loop L;          // batch loop: pdl 2 = c
   int *err;
+  int64_t tiles_n, tiles_m, batch;  // the output tiles: w, h, batch
 };
 
 __device__ __forceinline__ uint32_t su32(const void *p) {
@@ -168,10 +169,20 @@ __global__ void __launch_bounds__(320, 1)
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
 
-  const int z = blockIdx.z;
+  // Persistent: this CTA computes tiles blockIdx.x, blockIdx.x + gridDim.x,
+  // ... (w fastest, then h, then the batch: neighbouring CTAs share A
+  // tiles in L2).  The stage ring and the two TMEM buffers carry on across
+  // tiles, so the accumulator warps' stores of one tile overlap the MMAs of
+  // the next, and the set-up is paid once per CTA.
   const int nk = (int)(g.Kp / TC_BK);
-  const int64_t m0 = (int64_t)blockIdx.y * TC_M, n0 = (int64_t)blockIdx.x * TC_N;
-  // limb products (a limb, b limb), smallest first: each slab starts a fresh
+  const int npr = (nk + SPB - 1) / SPB;  // K-ranges (TMEM buffer uses) per tile
+  const int64_t tiles = g.tiles_n * g.tiles_m * g.batch;
+  auto coords = [&](int64_t t, int &z, int64_t &m0, int64_t &n0) {
+    n0 = (t % g.tiles_n) * TC_N;
+    m0 = ((t / g.tiles_n) % g.tiles_m) * TC_M;
+    z = (int)(t / (g.tiles_n * g.tiles_m));
+  };
+  // limb products (a limb, b limb), smallest first: each range starts a fresh
   // accumulator, so only the last (a0 b0) products are added at full size
   constexpr int PA3[6] = {2, 1, 0, 1, 0, 0}, PB3[6] = {0, 1, 2, 0, 1, 0};
   constexpr int PA2[3] = {1, 0, 0}, PB2[3] = {0, 1, 0};
@@ -180,92 +191,111 @@ __global__ void __launch_bounds__(320, 1)
   if (warp == 8) {
     if (lane == 0) {
       // -------------------------------------------------------- producer
-      const int za = g.nA == 1 ? 0 : z, zb = g.nB == 1 ? 0 : z;
-      for (int kb = 0; kb < nk && ok; kb++) {
-        const int s = kb % C::STAGES, use = kb / C::STAGES;
-        if (use > 0) ok = mbar_wait(&empty[s], (use - 1) & 1, g.err);
-        if (!ok) break;
-        uint8_t *st = base + s * C::STAGE_BYTES;
-        mbar_expect_tx(&full[s], C::STAGE_BYTES);
+      int64_t kg = 0;  // slabs loaded by this CTA so far
+      for (int64_t t = blockIdx.x; t < tiles && ok; t += gridDim.x) {
+        int z;
+        int64_t m0, n0;
+        coords(t, z, m0, n0);
+        const int za = g.nA == 1 ? 0 : z, zb = g.nB == 1 ? 0 : z;
+        for (int kb = 0; kb < nk && ok; kb++, kg++) {
+          const int s = (int)(kg % C::STAGES);
+          const int64_t use = kg / C::STAGES;
+          if (use > 0) ok = mbar_wait(&empty[s], (uint32_t)((use - 1) & 1), g.err);
+          if (!ok) break;
+          uint8_t *st = base + s * C::STAGE_BYTES;
+          mbar_expect_tx(&full[s], C::STAGE_BYTES);
 #pragma unroll
-        for (int l = 0; l < LIMBS; l++)
-          tma_load_2d(st + l * A_TILE, &tmA, &full[s], kb * TC_BK,
-                      (int)((l * g.nA + za) * g.M + m0));
+          for (int l = 0; l < LIMBS; l++)
+            tma_load_2d(st + l * A_TILE, &tmA, &full[s], kb * TC_BK,
+                        (int)((l * g.nA + za) * g.M + m0));
 #pragma unroll
-        for (int l = 0; l < LIMBS; l++)
-          tma_load_2d(st + LIMBS * A_TILE + l * B_TILE, &tmB, &full[s], kb * TC_BK,
-                      (int)((l * g.nB + zb) * g.N + n0));
+          for (int l = 0; l < LIMBS; l++)
+            tma_load_2d(st + LIMBS * A_TILE + l * B_TILE, &tmB, &full[s], kb * TC_BK,
+                        (int)((l * g.nB + zb) * g.N + n0));
+        }
       }
     }
   } else if (warp == 9) {
     if (lane == 0) {
       // ------------------------------------------------------------- MMA
-      for (int kb = 0; kb < nk && ok; kb++) {
-        const int s = kb % C::STAGES, use = kb / C::STAGES;
-        const int pr = kb / SPB, b = pr & 1, j = pr >> 1;
-        const bool opens = kb % SPB == 0, closes = kb % SPB == SPB - 1 || kb == nk - 1;
-        if (opens && j > 0) ok = mbar_wait(&acce[b], (j - 1) & 1, g.err);
-        if (ok) ok = mbar_wait(&full[s], use & 1, g.err);
-        if (!ok) break;
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const uint32_t st = su32(base + s * C::STAGE_BYTES);
-        const uint32_t d = tmem + (uint32_t)(b * TC_N);
-        int first = opens ? 1 : 0;
+      int64_t kg = 0, pbase = 0;  // slabs and K-ranges issued by this CTA so far
+      for (int64_t t = blockIdx.x; t < tiles && ok; t += gridDim.x, pbase += npr) {
+        for (int kb = 0; kb < nk && ok; kb++, kg++) {
+          const int s = (int)(kg % C::STAGES);
+          const int64_t use = kg / C::STAGES;
+          const int64_t pr = pbase + kb / SPB, j = pr >> 1;
+          const int b = (int)(pr & 1);
+          const bool opens = kb % SPB == 0, closes = kb % SPB == SPB - 1 || kb == nk - 1;
+          if (opens && j > 0) ok = mbar_wait(&acce[b], (uint32_t)((j - 1) & 1), g.err);
+          if (ok) ok = mbar_wait(&full[s], (uint32_t)(use & 1), g.err);
+          if (!ok) break;
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          const uint32_t st = su32(base + s * C::STAGE_BYTES);
+          const uint32_t d = tmem + (uint32_t)(b * TC_N);
+          int first = opens ? 1 : 0;
 #pragma unroll
-        for (int p = 0; p < C::NPROD; p++) {
+          for (int p = 0; p < C::NPROD; p++) {
 #pragma unroll
-          for (int ks = 0; ks < TC_BK / 16; ks++) {
-            const int pa = LIMBS == 3 ? PA3[p] : PA2[p], pb = LIMBS == 3 ? PB3[p] : PB2[p];
-            const uint64_t ad = sdesc_sw64(st + pa * A_TILE + ks * 32);
-            const uint64_t bd = sdesc_sw64(st + LIMBS * A_TILE + pb * B_TILE + ks * 32);
-            umma(d, ad, bd, first ? 0u : 1u);
-            first = 0;
+            for (int ks = 0; ks < TC_BK / 16; ks++) {
+              const int pa = LIMBS == 3 ? PA3[p] : PA2[p], pb = LIMBS == 3 ? PB3[p] : PB2[p];
+              const uint64_t ad = sdesc_sw64(st + pa * A_TILE + ks * 32);
+              const uint64_t bd = sdesc_sw64(st + LIMBS * A_TILE + pb * B_TILE + ks * 32);
+              umma(d, ad, bd, first ? 0u : 1u);
+              first = 0;
+            }
           }
+          umma_commit(&empty[s]);
+          if (closes) umma_commit(&accf[b]);
         }
-        umma_commit(&empty[s]);
-        if (closes) umma_commit(&accf[b]);
       }
     }
   } else {
     // ------------------------------------------- accumulators (warps 0-7)
     // warp w reads TMEM lanes 32*(w%4).. (its 32 rows) and columns
-    // 128*(w/4).. (its half of the tile), adding each slab with RN fp32.
+    // 128*(w/4).. (its half of the tile), adding each range with RN fp32,
+    // then stores its part of the tile.
     const int q = warp & 3, half = warp >> 2;
-    float acc[128];
-#pragma unroll
-    for (int i = 0; i < 128; i++) acc[i] = 0.f;
     const uint32_t tl = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(half * 128);
-    const int npr = (nk + SPB - 1) / SPB;
-    for (int pr = 0; pr < npr && ok; pr++) {
-      const int b = pr & 1;
-      if (lane == 0) ok = mbar_wait(&accf[b], (pr >> 1) & 1, g.err);
-      ok = __shfl_sync(0xffffffffu, ok, 0);  // warp-uniform for tcgen05.ld
-      if (!ok) break;
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    int64_t pbase = 0;
+    for (int64_t t = blockIdx.x; t < tiles && ok; t += gridDim.x, pbase += npr) {
+      int z;
+      int64_t m0, n0;
+      coords(t, z, m0, n0);
+      float acc[128];
 #pragma unroll
-      for (int c = 0; c < 4; c++) {
-        uint32_t r[32];
-        asm volatile(
-            "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-            "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-            "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
-              "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]),
-              "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]),
-              "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
-              "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]),
-              "=r"(r[30]), "=r"(r[31])
-            : "r"(tl + (uint32_t)(b * TC_N + c * 32)));
-        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      for (int i = 0; i < 128; i++) acc[i] = 0.f;
+      for (int r = 0; r < npr && ok; r++) {
+        const int64_t pr = pbase + r;
+        const int b = (int)(pr & 1);
+        if (lane == 0) ok = mbar_wait(&accf[b], (uint32_t)((pr >> 1) & 1), g.err);
+        ok = __shfl_sync(0xffffffffu, ok, 0);  // warp-uniform for tcgen05.ld
+        if (!ok) break;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 #pragma unroll
-        for (int i = 0; i < 32; i++) acc[c * 32 + i] = __fadd_rn(acc[c * 32 + i], __uint_as_float(r[i]));
+        for (int c = 0; c < 4; c++) {
+          uint32_t rg[32];
+          asm volatile(
+              "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+              "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+              "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+              : "=r"(rg[0]), "=r"(rg[1]), "=r"(rg[2]), "=r"(rg[3]), "=r"(rg[4]), "=r"(rg[5]),
+                "=r"(rg[6]), "=r"(rg[7]), "=r"(rg[8]), "=r"(rg[9]), "=r"(rg[10]), "=r"(rg[11]),
+                "=r"(rg[12]), "=r"(rg[13]), "=r"(rg[14]), "=r"(rg[15]), "=r"(rg[16]), "=r"(rg[17]),
+                "=r"(rg[18]), "=r"(rg[19]), "=r"(rg[20]), "=r"(rg[21]), "=r"(rg[22]), "=r"(rg[23]),
+                "=r"(rg[24]), "=r"(rg[25]), "=r"(rg[26]), "=r"(rg[27]), "=r"(rg[28]), "=r"(rg[29]),
+                "=r"(rg[30]), "=r"(rg[31])
+              : "r"(tl + (uint32_t)(b * TC_N + c * 32)));
+          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+          for (int i = 0; i < 32; i++)
+            acc[c * 32 + i] = __fadd_rn(acc[c * 32 + i], __uint_as_float(rg[i]));
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncwarp();
+        if (lane == 0)
+          asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(&acce[b])) : "memory");
       }
-      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-      __syncwarp();
-      if (lane == 0)
-        asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(&acce[b])) : "memory");
-    }
-    if (ok) {
+      if (!ok) break;
       int64_t offs[MAXP];
       loop_offsets(g.L, z, offs);
       float *C0 = reinterpret_cast<float *>(g.c) + offs[2];
@@ -487,15 +517,18 @@ pdlgb300_error tc_typed(const MMArgs &g, cudaStream_t s) {
     cudaFuncSetAttribute(k_mm_tc<LIMBS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::SMEM);
     attr_set[LIMBS] = true;
   }
-  dim3 grid((unsigned)((g.N + TC_N - 1) / TC_N), (unsigned)((g.M + TC_M - 1) / TC_M),
-            (unsigned)g.batch);
+  t.tiles_n = (g.N + TC_N - 1) / TC_N;
+  t.tiles_m = (g.M + TC_M - 1) / TC_M;
+  t.batch = g.batch;
+  // one CTA per SM (the stages take most of its shared memory), each walking
+  // tiles; a launch with fewer tiles than SMs has one tile per CTA
+  dim3 grid((unsigned)std::min<int64_t>(t.tiles_n * t.tiles_m * t.batch, (int64_t)nsm));
   k_mm_tc<LIMBS><<<grid, 320, C::SMEM, s>>>(mA, mB, t);
   if (!pgh::cuda_check(cudaGetLastError(), &e, "k_mm_tc")) {
     cudaFreeAsync(scratch, s);
     return e;
   }
-  pgh::record_kernel(LIMBS == 3 ? "k_mm_tc_bf16x6" : "k_mm_tc_bf16x3",
-                     (int64_t)grid.x * grid.y * grid.z, 320);
+  pgh::record_kernel(LIMBS == 3 ? "k_mm_tc_bf16x6" : "k_mm_tc_bf16x3", (int64_t)grid.x, 320);
   int herr = 0;
   cudaMemcpyAsync(&herr, errp, sizeof(int), cudaMemcpyDeviceToHost, s);
   cudaFreeAsync(scratch, s);
