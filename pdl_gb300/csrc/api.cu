@@ -1145,6 +1145,18 @@ pdlgb300_error dispatch_cumusum(RunCtx &c, int dop) {
     return launch_cumusum(dop, c.v[0].datatype, g, g_stream);
   }
   RET_IF(status_word(&g.err));
+  // Many rows of several chunks, equally wide types: a block per row walks
+  // its chunks in order (three blocks per SM; taken when the rows fill the
+  // resident blocks eight times or more, so that the last partial round of
+  // rows costs little)
+  const int64_t rch = scan_rowblk_chunk(dop, c.v[0].datatype);
+  if (rch > 0 && g.n >= 2 * rch && g.rows >= 8LL * 3 * nsm &&
+      chain_aligned(g.L, c.dev[0], c.dev[1], TSIZES[c.v[0].datatype], TSIZES[c.v[1].datatype])) {
+    g.mode = 4;
+    g.chunk = rch;
+    g.nchunk = (int)((g.n + rch - 1) / rch);
+    return launch_cumusum(dop, c.v[0].datatype, g, g_stream);
+  }
   // 16-byte aligned rows of 4- and 8-byte types, not too short: the chained
   // single-pass scan (one block per chunk, look-back across a row's chunks)
   const int64_t cch = scan_chain_chunk(dop, c.v[0].datatype, g.f32_comp);

@@ -185,7 +185,8 @@ struct ScanArgs {
   int nchunk;        // chunks per row (> 1: three-pass long-row scan)
   int64_t chunk;     // elements per chunk
   void *partials;    // per (row, chunk) totals, then exclusive carries
-  int mode;          // 0 full row, 1 chunk totals only, 2 chunk scan with carry, 3 chained
+  int mode;          // 0 full row, 1 chunk totals only, 2 chunk scan with carry, 3 chained,
+                     // 4 a block per row
   int *err;          // device status word: set when a bounded wait gives up
   void *status;      // chained scan: look-back slots (ChainSlot), a power of two
   uint64_t status_mask;
@@ -198,6 +199,8 @@ struct alignas(32) ChainSlot {
 };
 // elements per chunk of the chained scan for an input type (0: not used)
 int64_t scan_chain_chunk(int dop, int in_dt, int f32_comp);
+// elements per chunk of the row-block scan of many rows (0: not used)
+int64_t scan_rowblk_chunk(int dop, int in_dt);
 pdlgb300_error launch_cumusum(int dop, int in_dt, ScanArgs g, cudaStream_t s);
 size_t scan_acc_size(int dop, int in_dt, int f32_comp);
 

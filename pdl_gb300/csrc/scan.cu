@@ -2,9 +2,15 @@
 // b(n) = inclusive running sum of a(n); a bad element gives a bad output
 // and leaves the running sum unchanged.
 //
-// Contiguous rows run warp-synchronously, one warp per row (k_scan_warp);
-// long rows with few rows are cut into chunks whose totals are summed
-// first.  Strided rows: one thread per row in the reference's order.
+// Contiguous 16-byte aligned rows of 4- and 8-byte types: many rows of
+// equally wide types run a block per row (k_scan_rowblk: the row's 32 KiB
+// chunks in order, the carry in registers, the next load in flight); other
+// rows the chained single-pass scan (k_scan_chain: a block per chunk of
+// 64 KiB, or 32 KiB for 8-byte types, its carry found by decoupled
+// look-back across the row's earlier chunks).  Other contiguous rows run
+// warp-synchronously, one warp per row (k_scan_warp); long rows with few
+// rows are cut into chunks whose totals are summed first.  Strided rows:
+// one thread per row in the reference's order.
 #include "args.cuh"
 #include "f64sum.cuh"
 
@@ -347,57 +353,36 @@ __device__ __forceinline__ Acc chain_lookback(const ScanArgs &g, ChainSlot *slot
   return excl;
 }
 
-// The chunk's input stays in the swizzled tile (read once for the thread
-// totals, once for the running sums), so a thread holds no input registers
-// across the block barriers and more blocks fit on an SM to cover the
-// look-back latency.  Equal-width outputs overwrite their input slots; wider
-// outputs (float32 -> float64) use a second, larger tile.
-template <class In, class Out, int BM, int COMP>
-__global__ void __launch_bounds__(chain_threads<In, Out>(), (sizeof(In) == 4 && sizeof(Out) == 4) ? 3 : 4)
-    k_scan_chain(const ScanArgs g, int64_t u0) {
-  constexpr int CB = chain_threads<In, Out>();
+// Chunk geometry of the chained scans: CB threads, ITEMS = 128 / sizeof(In)
+// items per thread, one warp's 32 x ITEMS items in a 4 KiB swizzled tile
+// (a lane's 16-byte vector q sits in slot q ^ (lane & 7)).
+template <class In, int CB> struct ChainGeom {
+  static constexpr int ITEMS = 128 / sizeof(In);
+  static constexpr int VEC = 16 / sizeof(In);
+  static constexpr int NV = ITEMS / VEC;  // 8 input vectors per thread
+  static constexpr int WSPAN = 32 * ITEMS;
+  static constexpr int CH = (CB / 32) * WSPAN;
+  static constexpr int WIN_B = 32 * NV * 16;
+};
+
+// Start the load of unit u's chunk into a warp's input tile at sin: full
+// warp spans as 16-byte cp.async copies (not waited for here), the ragged
+// end of a row as plain loads with the identity past the row's end.
+template <class In, class Out, int COMP, int CB>
+__device__ __forceinline__ void chain_load(const ScanArgs &g, int64_t u, uint32_t sin, int lane,
+                                           int warp) {
   using S = ScanT<In, Out, COMP>;
-  using Acc = typename S::Acc;
-  constexpr int ITEMS = 128 / sizeof(In);                // per thread
-  constexpr int VEC = 16 / sizeof(In);
-  constexpr int NV = ITEMS / VEC;                        // 8 input vectors per thread
-  constexpr int VO = 16 / sizeof(Out);                   // outputs per 16-byte vector
-  constexpr int OV = ITEMS / VO;                         // output vectors per thread
-  constexpr int WSPAN = 32 * ITEMS;                      // elements per warp
-  constexpr int CH = (CB / 32) * WSPAN;                  // elements per chunk
-  constexpr int WIN_B = 32 * NV * 16;                    // input tile bytes per warp
-  constexpr int WOUT_B = OV == NV ? 0 : 32 * OV * 16;    // separate output tile per warp
-  static_assert(NV == 8 && (OV == 8 || OV == 16), "swizzle needs 8 or 16 slots per row");
-  extern __shared__ __align__(16) unsigned char sm_tile[];
-  __shared__ Acc s_w[CB / 32];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const uint32_t sin = (uint32_t)__cvta_generic_to_shared(sm_tile) + (uint32_t)(warp * WIN_B);
-  const uint32_t sout = OV == NV ? sin
-                                 : (uint32_t)__cvta_generic_to_shared(sm_tile) +
-                                       (uint32_t)((CB / 32) * WIN_B + warp * WOUT_B);
-  const int64_t u = u0 + blockIdx.x;
+  using GM = ChainGeom<In, CB>;
+  constexpr int NV = GM::NV, VEC = GM::VEC, ITEMS = GM::ITEMS;
   const int64_t row = u / g.nchunk;
   const int c = (int)(u - row * g.nchunk);
   int64_t offs[MAXP];
   loop_offsets(g.L, row, offs);
   const In *a = reinterpret_cast<const In *>(g.a) + offs[0];
-  const int64_t lo = (int64_t)c * CH;
-  const int64_t hi = lo + CH < g.n ? lo + CH : g.n;
-  const int64_t wlo = lo + (int64_t)warp * WSPAN;
-  const bool fast = wlo + WSPAN <= hi;
-  const In bad = from_bits<In>(g.abad);
-  auto slot_in = [&](int q) { return sin + (uint32_t)(lane * NV * 16 + ((q ^ (lane & 7)) * 16)); };
-  auto ldin = [&](int q, In (&x)[VEC]) {
-    float4 f;
-    asm volatile("ld.shared.v4.f32 {%0,%1,%2,%3}, [%4];"
-                 : "=f"(f.x), "=f"(f.y), "=f"(f.z), "=f"(f.w)
-                 : "r"(slot_in(q)));
-    memcpy(x, &f, 16);
-  };
-  int nvalid = ITEMS;  // items of this thread inside the row (slow path)
-  const int64_t t0 = wlo + (int64_t)lane * ITEMS;
-  if (fast) {
-    // striped 16-byte copies: vector q of lane L lands in row L, slot q ^ (L & 7)
+  const int64_t lo = (int64_t)c * GM::CH;
+  const int64_t hi = lo + GM::CH < g.n ? lo + GM::CH : g.n;
+  const int64_t wlo = lo + (int64_t)warp * GM::WSPAN;
+  if (wlo + GM::WSPAN <= hi) {
 #pragma unroll
     for (int r = 0; r < NV; r++) {
       const int gv = r * 32 + lane;
@@ -407,12 +392,10 @@ __global__ void __launch_bounds__(chain_threads<In, Out>(), (sizeof(In) == 4 && 
                    "l"(a + wlo + (int64_t)gv * VEC)
                    : "memory");
     }
-    asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;" ::: "memory");
-    __syncwarp();
   } else {
-    // the ragged end of a row: this thread's items, zero past the end
+    const int64_t t0 = wlo + (int64_t)lane * ITEMS;
     const int64_t left = hi - t0;
-    nvalid = left <= 0 ? 0 : (left >= ITEMS ? ITEMS : (int)left);
+    const int nvalid = left <= 0 ? 0 : (left >= ITEMS ? ITEMS : (int)left);
 #pragma unroll
     for (int q = 0; q < NV; q++) {
       In x[VEC];
@@ -420,10 +403,55 @@ __global__ void __launch_bounds__(chain_threads<In, Out>(), (sizeof(In) == 4 && 
       for (int e = 0; e < VEC; e++) x[e] = q * VEC + e < nvalid ? a[t0 + q * VEC + e] : S::pad();
       float4 f;
       memcpy(&f, x, 16);
-      asm volatile("st.shared.v4.f32 [%0], {%1,%2,%3,%4};" ::"r"(slot_in(q)), "f"(f.x),
-                   "f"(f.y), "f"(f.z), "f"(f.w)
+      const uint32_t dst = sin + (uint32_t)(lane * NV * 16 + ((q ^ (lane & 7)) * 16));
+      asm volatile("st.shared.v4.f32 [%0], {%1,%2,%3,%4};" ::"r"(dst), "f"(f.x), "f"(f.y),
+                   "f"(f.z), "f"(f.w)
                    : "memory");
     }
+  }
+}
+
+// Scan unit u's chunk from the warp's loaded input tile at sin: thread
+// totals, warp and block scans of the totals, the look-back across the
+// row's earlier chunks (warp 0, while the other warps wait at the block
+// barrier), the running sums written to the output tile at sout (the input
+// tile itself when the types are equally wide), then 16-byte streaming
+// stores.  Calls __syncthreads twice: every thread of the block runs it.
+//
+// LOOK false: the chunks of a row are scanned in order by one block, and the
+// exclusive prefix is `carry` (warp 0's, advanced here by the chunk total).
+template <class In, class Out, int BM, int COMP, int CB, bool LOOK = true>
+__device__ __forceinline__ void chain_body(const ScanArgs &g, int64_t u, uint32_t sin,
+                                           uint32_t sout, typename ScanT<In, Out, COMP>::Acc *s_w,
+                                           int lane, int warp,
+                                           typename ScanT<In, Out, COMP>::Acc &carry) {
+  using S = ScanT<In, Out, COMP>;
+  using Acc = typename S::Acc;
+  using GM = ChainGeom<In, CB>;
+  constexpr int ITEMS = GM::ITEMS, VEC = GM::VEC, NV = GM::NV;
+  constexpr int VO = 16 / sizeof(Out);  // outputs per 16-byte vector
+  constexpr int OV = ITEMS / VO;        // output vectors per thread
+  static_assert(NV == 8 && (OV == 8 || OV == 16), "swizzle needs 8 or 16 slots per row");
+  const int64_t row = u / g.nchunk;
+  const int c = (int)(u - row * g.nchunk);
+  const int64_t lo = (int64_t)c * GM::CH;
+  const int64_t hi = lo + GM::CH < g.n ? lo + GM::CH : g.n;
+  const int64_t wlo = lo + (int64_t)warp * GM::WSPAN;
+  const bool fast = wlo + GM::WSPAN <= hi;
+  const In bad = from_bits<In>(g.abad);
+  auto slot_in = [&](int q) { return sin + (uint32_t)(lane * NV * 16 + ((q ^ (lane & 7)) * 16)); };
+  auto ldin = [&](int q, In (&x)[VEC]) {
+    float4 f;
+    asm volatile("ld.shared.v4.f32 {%0,%1,%2,%3}, [%4];"
+                 : "=f"(f.x), "=f"(f.y), "=f"(f.z), "=f"(f.w)
+                 : "r"(slot_in(q)));
+    memcpy(x, &f, 16);
+  };
+  const int64_t t0 = wlo + (int64_t)lane * ITEMS;
+  int nvalid = ITEMS;  // items of this thread inside the row (ragged end)
+  if (!fast) {
+    const int64_t left = hi - t0;
+    nvalid = left <= 0 ? 0 : (left >= ITEMS ? ITEMS : (int)left);
   }
   // items past the row's end hold the identity and are never stored
   auto good = [&](In x) { return !is_bad<In, BM>(x, bad); };
@@ -479,7 +507,10 @@ __global__ void __launch_bounds__(chain_threads<In, Out>(), (sizeof(In) == 4 && 
     Acc wex = shfl_up_any(wt, 1);
     if (lane == 0) wex = S::zero();
     Acc excl = S::zero();
-    if (g.nchunk > 1) {
+    if constexpr (!LOOK) {
+      excl = carry;
+      carry = S::add(carry, agg);
+    } else if (g.nchunk > 1) {
       ChainSlot *slots = reinterpret_cast<ChainSlot *>(g.status);
       const uint64_t gid = g.gid_base + (uint64_t)u;
       if (c == 0) {
@@ -524,6 +555,8 @@ __global__ void __launch_bounds__(chain_threads<In, Out>(), (sizeof(In) == 4 && 
     }
   }
   __syncwarp();
+  int64_t offs[MAXP];
+  loop_offsets(g.L, row, offs);
   Out *b = reinterpret_cast<Out *>(g.b) + offs[1];
   if (fast) {
 #pragma unroll
@@ -555,6 +588,73 @@ __global__ void __launch_bounds__(chain_threads<In, Out>(), (sizeof(In) == 4 && 
       b[t0 + j] = o;
     }
   }
+  __syncwarp();
+}
+
+// One block per chunk.  The chunk's input stays in the swizzled tile (read
+// once for the thread totals, once for the running sums), so a thread holds
+// no input registers across the block barriers and more blocks fit on an SM
+// to cover the look-back latency.  Equal-width outputs overwrite their input
+// slots; wider outputs (float32 -> float64) use a second, larger tile.
+template <class In, class Out, int BM, int COMP>
+__global__ void __launch_bounds__(chain_threads<In, Out>(), (sizeof(In) == 4 && sizeof(Out) == 4) ? 3 : 4)
+    k_scan_chain(const ScanArgs g, int64_t u0) {
+  constexpr int CB = chain_threads<In, Out>();
+  using S = ScanT<In, Out, COMP>;
+  using GM = ChainGeom<In, CB>;
+  constexpr int OV = GM::ITEMS / (16 / sizeof(Out));
+  constexpr int WOUT_B = OV == GM::NV ? 0 : 32 * OV * 16;  // separate output tile per warp
+  extern __shared__ __align__(16) unsigned char sm_tile[];
+  __shared__ typename S::Acc s_w[CB / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t sin = (uint32_t)__cvta_generic_to_shared(sm_tile) + (uint32_t)(warp * GM::WIN_B);
+  const uint32_t sout = OV == GM::NV ? sin
+                                     : (uint32_t)__cvta_generic_to_shared(sm_tile) +
+                                           (uint32_t)((CB / 32) * GM::WIN_B + warp * WOUT_B);
+  const int64_t u = u0 + blockIdx.x;
+  chain_load<In, Out, COMP, CB>(g, u, sin, lane, warp);
+  asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;" ::: "memory");
+  __syncwarp();
+  typename S::Acc carry = S::zero();
+  chain_body<In, Out, BM, COMP, CB>(g, u, sin, sout, s_w, lane, warp, carry);
+}
+
+// Many rows of equally wide types: one block per row walks the row's
+// chunks in order, the carry in warp 0's registers (no look-back, no
+// flags), the next chunk's load in flight while the current one is scanned.
+// Blocks of 256 threads and two 32 KiB tiles: three blocks per SM, three
+// independent rows in progress on each.
+constexpr int ROWBLK_CB = 256;
+template <class In> constexpr size_t rowblk_smem() { return (size_t)2 * ROWBLK_CB * 128; }
+
+template <class In, class Out, int BM, int COMP>
+__global__ void __launch_bounds__(ROWBLK_CB, 3) k_scan_rowblk(const ScanArgs g) {
+  static_assert(sizeof(In) == sizeof(Out), "the tiles hold equal-width outputs in place");
+  using S = ScanT<In, Out, COMP>;
+  constexpr int CB = ROWBLK_CB;
+  using GM = ChainGeom<In, CB>;
+  constexpr uint32_t STAGE_B = (uint32_t)CB * 128;
+  extern __shared__ __align__(16) unsigned char sm_tile[];
+  __shared__ typename S::Acc s_w[CB / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t base = (uint32_t)__cvta_generic_to_shared(sm_tile) + (uint32_t)(warp * GM::WIN_B);
+  for (int64_t row = blockIdx.x; row < g.rows; row += gridDim.x) {
+    const int64_t u0 = row * g.nchunk;
+    chain_load<In, Out, COMP, CB>(g, u0, base, lane, warp);
+    asm volatile("cp.async.commit_group;" ::: "memory");
+    typename S::Acc carry = S::zero();
+    for (int c = 0; c < g.nchunk; c++) {
+      const uint32_t t = base + (uint32_t)(c & 1) * STAGE_B;
+      // the other tile held chunk c - 1, read and stored already
+      if (c + 1 < g.nchunk)
+        chain_load<In, Out, COMP, CB>(g, u0 + c + 1, base + (uint32_t)((c + 1) & 1) * STAGE_B,
+                                      lane, warp);
+      asm volatile("cp.async.commit_group;\ncp.async.wait_group 1;" ::: "memory");
+      __syncwarp();
+      chain_body<In, Out, BM, COMP, CB, false>(g, u0 + c, t, t, s_w, lane, warp, carry);
+    }
+  }
+  asm volatile("cp.async.wait_group 0;" ::: "memory");
 }
 
 // One thread per row, any increments, the reference's order.
@@ -625,6 +725,32 @@ pdlgb300_error scan_chain_typed(ScanArgs g, cudaStream_t s) {
   return e;
 }
 
+template <class In, class Out, int COMP>
+pdlgb300_error scan_rowblk_typed(ScanArgs g, cudaStream_t s) {
+  pdlgb300_error e = pgh::ok();
+  if constexpr (sizeof(In) == sizeof(Out) && chain_ok<In, Out>()) {
+    constexpr size_t smem = rowblk_smem<In>();
+    static bool attr = false;
+    if (!attr) {
+      for (void *k : {(void *)k_scan_rowblk<In, Out, 0, COMP>, (void *)k_scan_rowblk<In, Out, 1, COMP>,
+                      (void *)k_scan_rowblk<In, Out, 2, COMP>}) {
+        cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+      }
+      attr = true;
+    }
+    const int grid = (int)std::min<int64_t>(g.rows, (int64_t)1 << 30);
+    if (!g.bad) k_scan_rowblk<In, Out, 0, COMP><<<grid, ROWBLK_CB, smem, s>>>(g);
+    else if (g.abad_isnan) k_scan_rowblk<In, Out, 2, COMP><<<grid, ROWBLK_CB, smem, s>>>(g);
+    else k_scan_rowblk<In, Out, 1, COMP><<<grid, ROWBLK_CB, smem, s>>>(g);
+    if (!pgh::cuda_check(cudaGetLastError(), &e, "k_scan_rowblk")) return e;
+    pgh::record_kernel("k_scan_rowblk", grid, ROWBLK_CB);
+  } else {
+    e = pgh::err(PDLGB300_EFATAL, "row-block scan: unsupported type pair");
+  }
+  return e;
+}
+
 template <class In, class Out> constexpr int64_t chain_chunk() {
   if constexpr (chain_ok<In, Out>()) return (int64_t)chain_threads<In, Out>() * (128 / sizeof(In));
   return 0;
@@ -634,6 +760,7 @@ template <class In, class Out, int COMP>
 pdlgb300_error scan_typed(ScanArgs g, cudaStream_t s) {
   pdlgb300_error e = pgh::ok();
   if (g.rows == 0) return e;
+  if (g.mode == 4) return scan_rowblk_typed<In, Out, COMP>(g, s);
   if (g.status || g.mode == 3) return scan_chain_typed<In, Out, COMP>(g, s);
   const int nsm = pgh::num_sms();
   if (g.mode < 0) {  // thread kernel
@@ -683,6 +810,22 @@ pdlgb300_error launch_cumusum(int dop, int in_dt, ScanArgs g, cudaStream_t s) {
     return scan_typed<In, OutP, 0>(g, s);
   });
   return pgh::err(PDLGB300_EUSERERROR, "cumusumover: unsupported type %d", in_dt);
+}
+
+// elements per chunk of the row-block scan (0: not used for this op/type)
+int64_t scan_rowblk_chunk(int dop, int in_dt) {
+  int64_t r = 0;
+  PG_DISPATCH(in_dt, {
+    using In = typename TT<DT>::T;
+    using OutP = typename TT<intplus(DT)>::T;
+    if (dop == 1 || dop == 3) {
+      if constexpr (sizeof(In) == sizeof(double) && chain_ok<In, double>())
+        r = (int64_t)ROWBLK_CB * (128 / sizeof(In));
+    } else if constexpr (sizeof(In) == sizeof(OutP) && chain_ok<In, OutP>()) {
+      r = (int64_t)ROWBLK_CB * (128 / sizeof(In));
+    }
+  });
+  return r;
 }
 
 int64_t scan_chain_chunk(int dop, int in_dt, int comp) {

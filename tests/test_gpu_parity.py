@@ -382,6 +382,26 @@ def test_chained_scan_bad_values(gpu, t, nanbad):
     assert_same(got, exp, rtol=rtol, atol=atol, scale=scale, what=f"cumusumover {t} bad nan={nanbad}")
 
 
+@pytest.mark.parametrize("t,n,rows", [("float", 16_400, 3700), ("double", 8_194, 3700),
+                                      ("long", 16_384, 3700)])
+def test_row_block_scan_many_rows(gpu, t, n, rows):
+    """Many rows of equally wide types run a block per row, the row's chunks
+    in order with the carry in registers (two or more chunks per row,
+    ragged row ends, 1 % BAD); float32 into float64 (dcumusumover) keeps the
+    chained scan."""
+    rng = seeded(n + rows + 7)
+    a, bad = rand_array(rng, t, (rows, n), -10, 10, bad_frac=0.01)
+    x = to_pdl(a, t, badflag=True)
+    got, exp = _run_both("cumusumover", [x])
+    assert P.last_launch_info()["kernel"] == "k_scan_rowblk"
+    clean = np.where(bad, 0, a)
+    rtol, atol, scale = _tol("cumusumover", clean, exp, exp.type) if exp.type in FLOAT_TYPES else (0, 0, None)
+    assert_same(got, exp, rtol=rtol, atol=atol, scale=scale, what=f"cumusumover {t} {rows}x{n}")
+    if t == "float":
+        P.dcumusumover(x)
+        assert P.last_launch_info()["kernel"] == "k_scan_chain"
+
+
 def test_chained_scan_unaligned_rows_fall_back(gpu):
     """Rows whose starts are not 16-byte aligned take the warp kernel."""
     rng = seeded(22)
