@@ -55,8 +55,10 @@ WORKLOAD = ("PDL::Ufunc sumover/average/cumusumover over dim 0 of float32 dims (
 FAMILY = "float64 dims (4096,2048) uniform[-1,1) seed 1, no bad values"
 # dram__bytes_read.sum + dram__bytes_write.sum per launch of the dominant
 # kernel on this workload, from the ncu captures summarised in profiles/
-# (captured at 1024 rows and scaled by 4 to the 4096-row matrix)
-NCU_TRAFFIC = {"cumusumover[matrix]": 4 * (268.610304e6 + 207.915008e6)}
+# (k_scan_rowblk captured at 3648 rows, scaled by 4096/3648 to the matrix;
+# k_scan_chain on the 2^27 row as captured)
+NCU_TRAFFIC = {"cumusumover[matrix]": (956.519168e6 + 924.768256e6) * 4096 / 3648,
+               "cumusumover[row]": 537.38e6 + 476.43e6}
 
 
 def peaks():
