@@ -839,6 +839,25 @@ def bench_sort(args, P, torch, stream, hbm):
         "ms": ms, "rows_per_s": 4096 / (ms * 1e-3), "gbs_in": al.nbytes / (ms * 1e-3) / 1e9,
         "kernel": "k_sortred_block", "error_vs_oracle": errs(r.numpy()[:256], want)}
     del r, xl
+    # one long row: the median of a whole float32 array of 2^22 values (the
+    # merge sort), against the oracle's quicksort of the same row on one core
+    aw = np.random.default_rng(13).standard_normal(1 << 22, dtype=np.float32)
+    xw = P.pdl(aw).to_device()
+    for op in ("medover", "qsort"):
+        r = getattr(P, op)(xw)
+        P.sync()
+        ms = time_op(torch, stream, lambda: getattr(P, op)(xw), 5)
+        t0 = time.perf_counter()
+        want = O.run(op, [P.pdl(aw)])[0].numpy()
+        el = time.perf_counter() - t0
+        out[f"{op}_one_row_of_2e22"] = {
+            "config": "float32 dims (4194304) N(0,1) seed 13: one row",
+            "ms": ms, "gbs_in": aw.nbytes / (ms * 1e-3) / 1e9,
+            "kernel": "k_lsort_tile + k_lsort_merge + k_lsort_finish",
+            "error_vs_oracle": errs(np.atleast_1d(r.numpy()), np.atleast_1d(want)),
+            "cpu_port_ms": el * 1e3}
+        del r
+    del xw
     # vector sorts: 512 planes of 2048 points in 3-D (float64, N(0,1), seed 11)
     v = np.random.default_rng(11).standard_normal((512, 2048, 3))
     xv = P.pdl(v).to_device()

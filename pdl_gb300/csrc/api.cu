@@ -1242,7 +1242,9 @@ pdlgb300_error dispatch_sortred(RunCtx &c, int kind) {
   if (g.rows == 0 || g.n == 0) return ok();
   void *scratch = nullptr;
   if (g.n > SORT_SHARED_MAXN) {  // (shorter rows sort in shared memory)
-    const size_t vbytes = ((size_t)g.rows * g.n * TSIZES[dt] + 15) & ~(size_t)15;
+    const size_t vbytes = ((kind == SR_QSORTI ? (size_t)g.rows * g.n * TSIZES[dt]
+                                              : sortred_long_scratch(g.rows, g.n, TSIZES[dt])) +
+                           15) & ~(size_t)15;
     const size_t ibytes = kind == SR_QSORTI ? (size_t)g.rows * g.n * sizeof(int64_t) : 0;
     RET_IF(dalloc(vbytes + ibytes, &scratch));
     g.scratch = scratch;

@@ -7,14 +7,18 @@
 // the two scans, swap, then the ranges [a,j] and [i,b]).  Its results are
 // not those of every sort: the order of equal keys in qsorti, the placement
 // of NaN, and which of -0 and +0 comes first all follow from the steps it
-// takes.  So each row runs the same steps here, one thread per row over a
-// private copy of the row in device scratch: the results are the
-// reference's in every case.  The two ranges after a partition are
+// takes.  So wherever the result could depend on the sort, a row runs the
+// same steps here, one thread over a private copy of the row: the results
+// are the reference's in every case.  Everywhere else a faster sort gives
+// the same array: rows up to 8192 sort in shared memory (a warp or a block
+// per row), longer rows of the value functions by a device-wide merge sort.  The two ranges after a partition are
 // disjoint, so sorting the smaller one first (an explicit stack, at most
 // 64 entries) and continuing with the larger one gives the same array.
 // Scans are bounded by their range (they cannot leave it: the pivot and the
 // elements swapped behind the scans stop them); a violation sets an error
 // bit and ends the row.
+#include <limits>
+
 #include "args.cuh"
 
 namespace pg {
@@ -535,6 +539,199 @@ __global__ void __launch_bounds__(SB_THREADS) k_sortred_block(const SortArgs g) 
   }
 }
 
+// Rows longer than SB_MAX, value functions (all but qsorti, whose order of
+// equal keys is the quicksort's own): a device-wide merge sort.  Where the
+// row's good values hold no NaN and not both -0 and +0, equal values are
+// equal bits and the sorted row is the same whatever sorts it.
+// * k_lsort_tile: each block takes a tile of LS_TILE elements of a row,
+//   puts a top value (above every good value) in place of bad elements and
+//   past the row's end, sorts the tile with a bitonic network in shared
+//   memory, and counts the row's good values and notes NaN and zero signs.
+// * k_lsort_merge: merge passes, runs of w -> 2w, each thread 8 outputs
+//   found by a merge-path search (equal values: the first run's first).
+// * k_lsort_finish: the outputs from the sorted good prefix; a row with
+//   NaN or both zeros is sorted again by one thread with the reference's
+//   quicksort over its elements in their order, as k_sortred does.
+constexpr int LS_TILE = 4096, LS_THREADS = 512, LS_PER = 8, LS_MT = 256, LS_FT = 256;
+
+template <class T> __device__ __forceinline__ T ls_top() {
+  if constexpr (std::is_floating_point_v<T>) return (T)INFINITY;
+  else return std::numeric_limits<T>::max();
+}
+constexpr int LS_NAN = 1, LS_NEG0 = 2, LS_POS0 = 4;
+
+template <class T, int K, bool BAD>
+__global__ void __launch_bounds__(LS_THREADS) k_lsort_tile(const SortArgs g, int64_t np, T *buf,
+                                                           unsigned long long *cnt, int *flags) {
+  __shared__ T sv[LS_TILE];
+  __shared__ int s_good, s_fl;
+  const Bad<T> bv{from_bits<T>(g.abad), (bool)g.abad_isnan};
+  const int64_t tiles = np / LS_TILE;
+  const int tid = threadIdx.x;
+  for (int64_t bt = blockIdx.x; bt < g.rows * tiles; bt += gridDim.x) {
+    const int64_t row = bt / tiles, t0 = (bt - row * tiles) * LS_TILE;
+    int64_t offs[MAXP];
+    loop_offsets(g.L, row, offs);
+    const T *a = reinterpret_cast<const T *>(g.a) + offs[0];
+    if (tid == 0) {
+      s_good = 0;
+      s_fl = 0;
+    }
+    __syncthreads();
+    int good = 0, fl = 0;
+    for (int i = tid; i < LS_TILE; i += LS_THREADS) {
+      const int64_t idx = t0 + i;
+      T v = ls_top<T>();
+      if (idx < g.n) {
+        const T x = a[idx * g.inc_a];
+        if (!(K != SR_MODE && BAD && bv.is(x))) {
+          v = x;
+          good++;
+          if constexpr (std::is_floating_point_v<T>) {
+            if (x != x) fl |= LS_NAN;
+            else if (x == (T)0) fl |= signbit(x) ? LS_NEG0 : LS_POS0;
+          }
+        }
+      }
+      sv[i] = v;
+    }
+    if (good) atomicAdd(&s_good, good);
+    if (fl) atomicOr(&s_fl, fl);
+    __syncthreads();
+    // bitonic network, ascending (with NaN the order is not used)
+    for (int k = 2; k <= LS_TILE; k <<= 1) {
+      for (int j = k >> 1; j > 0; j >>= 1) {
+#pragma unroll
+        for (int q = 0; q < LS_TILE / (2 * LS_THREADS); q++) {
+          const int pi = q * LS_THREADS + tid;              // pair index
+          const int i = ((pi / j) * 2 * j) + (pi % j), ixj = i + j;
+          const bool up = (i & k) == 0;
+          const T x = sv[i], y = sv[ixj];
+          if ((y < x) == up) {
+            sv[i] = y;
+            sv[ixj] = x;
+          }
+        }
+        __syncthreads();
+      }
+    }
+    T *o = buf + row * np + t0;
+    for (int i = tid; i < LS_TILE; i += LS_THREADS) o[i] = sv[i];
+    if (tid == 0) {
+      if (s_good) atomicAdd(&cnt[row], (unsigned long long)s_good);
+      if (s_fl) atomicOr(&flags[row], s_fl);
+    }
+    __syncthreads();
+  }
+}
+
+template <class T>
+__global__ void __launch_bounds__(LS_MT) k_lsort_merge(const T *in, T *out, int64_t np, int64_t w,
+                                                       int64_t rows) {
+  const int64_t per_row = np / LS_PER;
+  for (int64_t q = (int64_t)blockIdx.x * LS_MT + threadIdx.x; q < rows * per_row;
+       q += (int64_t)gridDim.x * LS_MT) {
+    const int64_t row = q / per_row, o = (q - row * per_row) * LS_PER;
+    const T *r = in + row * np;
+    const int64_t p0 = o / (2 * w) * (2 * w);
+    const int64_t a1 = p0 + w < np ? p0 + w : np, b1 = p0 + 2 * w < np ? p0 + 2 * w : np;
+    const T *A = r + p0, *B = r + a1;
+    const int64_t na = a1 - p0, nb = b1 - a1, d = o - p0;
+    int64_t lo = d - nb > 0 ? d - nb : 0, hi = d < na ? d : na;
+    while (lo < hi) {  // A elements among the first d outputs
+      const int64_t mid = (lo + hi) >> 1;
+      if (!(B[d - 1 - mid] < A[mid])) lo = mid + 1;
+      else hi = mid;
+    }
+    int64_t i = lo, j = d - lo;
+    T *dst = out + row * np + o;
+#pragma unroll
+    for (int e = 0; e < LS_PER; e++) {
+      const bool takeA = j >= nb || (i < na && !(B[j] < A[i]));
+      dst[e] = takeA ? A[i++] : B[j++];
+    }
+  }
+}
+
+template <class T, int K, bool BAD>
+__global__ void __launch_bounds__(LS_FT) k_lsort_finish(const SortArgs g, const T *sorted,
+                                                        T *spare, int64_t np,
+                                                        const unsigned long long *cnt,
+                                                        const int *flags, int64_t chunks) {
+  const Bad<T> bv{from_bits<T>(g.abad), (bool)g.abad_isnan};
+  const T obad = from_bits<T>(g.obad);
+  for (int64_t bc = blockIdx.x; bc < g.rows * chunks; bc += gridDim.x) {
+    const int64_t row = bc / chunks, ch = bc - row * chunks;
+    int64_t offs[MAXP];
+    loop_offsets(g.L, row, offs);
+    T *out = reinterpret_cast<T *>(g.b) + offs[g.out_pdl];
+    const int fl = flags[row];
+    const bool unsafe = (fl & LS_NAN) || ((fl & LS_NEG0) && (fl & LS_POS0));
+    if (unsafe) {
+      if (ch == 0 && threadIdx.x == 0) {
+        const T *a = reinterpret_cast<const T *>(g.a) + offs[0];
+        T *tmp = spare + row * np;
+        int64_t nn = 0;
+        for (int64_t t = 0; t < g.n; t++) {
+          const T v = a[t * g.inc_a];
+          if (K != SR_MODE && BAD && bv.is(v)) continue;
+          tmp[nn++] = v;
+        }
+        if (nn > 0 && !qs_values<T>(tmp, 0, nn - 1)) atomicOr(g.err, 1);
+        finish_values<T, K>(g, tmp, nn, offs, out, obad, 0, 1);
+      }
+      continue;
+    }
+    const int64_t nn = (int64_t)cnt[row];
+    const T *v = sorted + row * np;
+    if constexpr (K == SR_QSORT) {
+      const int64_t lo = ch * (int64_t)LS_TILE, hi = lo + LS_TILE < g.n ? lo + LS_TILE : g.n;
+      for (int64_t t = lo + threadIdx.x; t < hi; t += LS_FT) out[t * g.inc_b] = t < nn ? v[t] : obad;
+    } else if (ch == 0) {
+      finish_values<T, K>(g, v, nn, offs, out, obad, threadIdx.x, LS_FT);
+    }
+  }
+}
+
+// scratch of the long-row merge sort: two buffers of rows x np values,
+// then the rows' good counts and flags
+int64_t lsort_np(int64_t n) { return (n + LS_TILE - 1) / LS_TILE * LS_TILE; }
+
+template <class T, int K>
+pdlgb300_error go_lsort(const SortArgs &g, cudaStream_t s) {
+  pdlgb300_error e = pgh::ok();
+  const int nsm = pgh::num_sms();
+  const int64_t np = lsort_np(g.n), tiles = np / LS_TILE;
+  T *b0 = reinterpret_cast<T *>(g.scratch);
+  T *b1 = b0 + g.rows * np;
+  unsigned long long *cnt = reinterpret_cast<unsigned long long *>(b1 + g.rows * np);
+  int *flags = reinterpret_cast<int *>(cnt + g.rows);
+  if (!pgh::cuda_check(cudaMemsetAsync(cnt, 0, (size_t)g.rows * (sizeof *cnt + sizeof *flags), s),
+                       &e, "lsort counters"))
+    return e;
+  const int64_t gt = std::max<int64_t>(1, std::min<int64_t>(g.rows * tiles, (int64_t)nsm * 16));
+  if (g.bad) k_lsort_tile<T, K, true><<<(int)gt, LS_THREADS, 0, s>>>(g, np, b0, cnt, flags);
+  else k_lsort_tile<T, K, false><<<(int)gt, LS_THREADS, 0, s>>>(g, np, b0, cnt, flags);
+  if (!pgh::cuda_check(cudaGetLastError(), &e, "k_lsort_tile")) return e;
+  pgh::record_kernel("k_lsort_tile", gt, LS_THREADS);
+  T *cur = b0, *nxt = b1;
+  const int64_t gm = std::max<int64_t>(
+      1, std::min<int64_t>((g.rows * (np / LS_PER) + LS_MT - 1) / LS_MT, (int64_t)nsm * 32));
+  for (int64_t w = LS_TILE; w < np; w *= 2) {
+    k_lsort_merge<T><<<(int)gm, LS_MT, 0, s>>>(cur, nxt, np, w, g.rows);
+    if (!pgh::cuda_check(cudaGetLastError(), &e, "k_lsort_merge")) return e;
+    pgh::record_kernel("k_lsort_merge", gm, LS_MT);
+    std::swap(cur, nxt);
+  }
+  const int64_t chunks = K == SR_QSORT ? tiles : 1;
+  const int64_t gf = std::max<int64_t>(1, std::min<int64_t>(g.rows * chunks, (int64_t)nsm * 16));
+  if (g.bad) k_lsort_finish<T, K, true><<<(int)gf, LS_FT, 0, s>>>(g, cur, nxt, np, cnt, flags, chunks);
+  else k_lsort_finish<T, K, false><<<(int)gf, LS_FT, 0, s>>>(g, cur, nxt, np, cnt, flags, chunks);
+  if (!pgh::cuda_check(cudaGetLastError(), &e, "k_lsort_finish")) return e;
+  pgh::record_kernel("k_lsort_finish", gf, LS_FT);
+  return e;
+}
+
 // dynamic shared memory of k_sortred_block for rows of n values of tsize bytes
 size_t sortred_block_smem(int64_t n, int tsize) {
   int64_t P = 1;
@@ -570,6 +767,7 @@ pdlgb300_error go_sort(const SortArgs &g, cudaStream_t s) {
     return e;
   }
   if (!g.scratch) return pgh::err(PDLGB300_EFATAL, "sort: no scratch for long rows");
+  if constexpr (K != SR_QSORTI) return go_lsort<T, K>(g, s);
   const int64_t grid = std::max<int64_t>(1, std::min<int64_t>((g.rows + 127) / 128, (int64_t)nsm * 16));
   if (g.bad) k_sortred<T, K, true><<<(int)grid, 128, 0, s>>>(g);
   else k_sortred<T, K, false><<<(int)grid, 128, 0, s>>>(g);
@@ -596,6 +794,10 @@ pdlgb300_error sort_family(int k, const SortArgs &g, cudaStream_t s) {
 }
 
 }  // namespace
+
+size_t sortred_long_scratch(int64_t rows, int64_t n, int tsize) {
+  return (size_t)2 * rows * lsort_np(n) * tsize + (size_t)rows * (sizeof(unsigned long long) + sizeof(int));
+}
 
 pdlgb300_error launch_sortred(int k, int dt, const SortArgs &g, cudaStream_t s) {
   PG_DISPATCH(dt, return sort_family<DT>(k, g, s));

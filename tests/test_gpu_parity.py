@@ -920,8 +920,8 @@ def test_sort_based_empty_and_errors(gpu):
 @pytest.mark.parametrize("op", SORT_OPS + ["pctover", "modeover"])
 def test_sort_based_long_rows(gpu, op, t):
     """Rows of 513 to 8192 elements (a block per row in shared memory) and
-    beyond (one thread per row): ties, NaN and signed zeros, distinct
-    values (the network), bad values."""
+    beyond (the merge sort, or for qsorti one thread per row): ties, NaN and
+    signed zeros, distinct values (the network), bad values."""
     if op == "modeover" and t in ("float", "double"):
         return
     rng = seeded(("sortlong", op, t))
@@ -940,6 +940,43 @@ def test_sort_based_long_rows(gpu, op, t):
         ins = [x, P.pdl(np.array(0.37))] if op == "pctover" else [x]
         got, exp = _run_both(op, ins)
         _bits_equal(got, exp, f"{op} {t} bad n=3000")
+
+
+@pytest.mark.parametrize("t", ["byte", "ushort", "long", "longlong", "float", "double"])
+@pytest.mark.parametrize("op", ["qsort", "medover", "oddmedover", "pctover", "oddpctover",
+                                "modeover"])
+def test_sort_based_rows_beyond_shared_memory(gpu, op, t):
+    """Rows longer than 8192 values: a merge sort (tiles of 4096 sorted in
+    shared memory, then merge passes) wherever the good values hold no NaN
+    and not both zeros; other rows sorted again with the reference's
+    quicksort.  Ties, bad values, ragged lengths, several rows, a row of
+    2^20; bit for bit against the oracle."""
+    if op == "modeover" and t in ("float", "double"):
+        return
+    rng = seeded(("lsort", op, t))
+    fl = t in ("float", "double")
+    cases = []
+    a, _ = rand_array(rng, t, (3, 20_001), -50, 50, bad_frac=0.0 if op == "modeover" else 0.05)
+    if fl:  # ties, and zeros of one sign only
+        a = np.where(a == P.default_badvalue(type_code(t)), a, np.round(a))
+        a = np.where(a == 0, np.zeros_like(a), a)
+    cases.append((a, op != "modeover"))
+    cases.append((rand_array(rng, t, (2, 100_003), -1000, 1000)[0], False))
+    if t in ("long", "float"):
+        cases.append((rand_array(rng, t, (1, 1 << 20), -1e6, 1e6)[0], False))
+    if fl:  # NaN in one row, both zeros in the other: the quicksort's order
+        b, _ = rand_array(rng, t, (2, 9_001), -3, 3)
+        b = np.round(b)
+        b[0, ::97] = np.nan
+        b[1, ::89] = -0.0
+        b[1, 1::89] = 0.0
+        cases.append((b, False))
+    for a, bf in cases:
+        x = to_pdl(a, t, badflag=bf)
+        ins = [x, P.pdl(np.array(0.37))] if op in ("pctover", "oddpctover") else [x]
+        got, exp = _run_both(op, ins)
+        assert P.last_launch_info()["kernel"] == "k_lsort_finish"
+        _bits_equal(got, exp, f"{op} {t} {a.shape} bad={bf}")
 
 
 @pytest.mark.parametrize("where", ["host", "device"])
