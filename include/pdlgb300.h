@@ -42,6 +42,10 @@ typedef enum pdlgb300_datatype {
 /* Error kinds, mirroring PDL_ENONE / PDL_EUSERERROR / PDL_EFATAL. */
 enum { PDLGB300_ENONE = 0, PDLGB300_EUSERERROR = 1, PDLGB300_EFATAL = 2 };
 
+/* Replaces pdl_error (lib/PDL/Core/pdl.h.PL:370-379).  PDL's needs_free
+ * says whether the caller frees the message; here the library always owns
+ * it (a per-thread buffer), so there is nothing to free.  The XS glue
+ * copies the text into croak() before the next library call. */
 typedef struct pdlgb300_error {
   int32_t error;       /* PDLGB300_ENONE on success */
   int32_t reserved;

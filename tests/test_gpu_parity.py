@@ -979,6 +979,44 @@ def test_sort_based_rows_beyond_shared_memory(gpu, op, t):
         _bits_equal(got, exp, f"{op} {t} {a.shape} bad={bf}")
 
 
+@pytest.mark.parametrize("op", ["qsort", "medover", "pctover"])
+def test_sort_beyond_shared_memory_edges(gpu, op):
+    """The merge sort at its edges: one past the shared-memory limit, whole
+    tiles, rows read with a stride (a transposed view), a strided qsort
+    output."""
+    rng = seeded(("lsort-edge", op))
+    for shape in [(2, 8193), (3, 12288)]:
+        a, _ = rand_array(rng, "double", shape, -100, 100)
+        x = to_pdl(a, "double")
+        ins = [x, P.pdl(np.array(0.61))] if op == "pctover" else [x]
+        got, exp = _run_both(op, ins)
+        _bits_equal(got, exp, f"{op} {shape}")
+    a, _ = rand_array(rng, "float", (20_000, 3), -100, 100)
+    v = to_pdl(a, "float").xchg(0, 1)       # 3 rows of 20000, increment 3
+    ins = [v, P.pdl(np.array(0.61))] if op == "pctover" else [v]
+    got, exp = _run_both(op, ins)
+    assert P.last_launch_info()["kernel"] == "k_lsort_finish"
+    _bits_equal(got, exp, f"{op} strided rows")
+
+
+def test_row_block_scan_strided_rows(gpu):
+    """The block-per-row scan over every other row of a matrix (a row
+    increment of two rows), and into an output slice of a larger array."""
+    rng = seeded("rowblk-stride")
+    a, _ = rand_array(rng, "float", (7400, 16_400), -10, 10)
+    x = to_pdl(a, "float").slice(slice(None), slice(0, None, 2))   # rows 0, 2, 4, ...
+    got, exp = _run_both("cumusumover", [x])
+    assert P.last_launch_info()["kernel"] == "k_scan_rowblk"
+    rtol, atol, scale = _tol("cumusumover", x.numpy(), exp, exp.type)
+    assert_same(got, exp, rtol=rtol, atol=atol, scale=scale, what="cumusumover every other row")
+    big = P.pdl(np.zeros((7400, 16_400), np.float32))
+    out = big.slice(slice(None), slice(1, None, 2))
+    P.cumusumover(x, out)
+    assert P.last_launch_info()["kernel"] == "k_scan_rowblk"
+    assert np.array_equal(out.numpy(), got.numpy())
+    assert not big.numpy()[0::2].any()
+
+
 @pytest.mark.parametrize("where", ["host", "device"])
 def test_in_place_outputs(gpu, where):
     """An output that is one of the inputs (PDL's Inplace => 1: the binary
