@@ -1242,13 +1242,8 @@ pdlgb300_error dispatch_sortred(RunCtx &c, int kind) {
   if (g.rows == 0 || g.n == 0) return ok();
   void *scratch = nullptr;
   if (g.n > SORT_SHARED_MAXN) {  // (shorter rows sort in shared memory)
-    const size_t vbytes = ((kind == SR_QSORTI ? (size_t)g.rows * g.n * TSIZES[dt]
-                                              : sortred_long_scratch(g.rows, g.n, TSIZES[dt])) +
-                           15) & ~(size_t)15;
-    const size_t ibytes = kind == SR_QSORTI ? (size_t)g.rows * g.n * sizeof(int64_t) : 0;
-    RET_IF(dalloc(vbytes + ibytes, &scratch));
+    RET_IF(dalloc(sortred_long_scratch(kind, g.rows, g.n, TSIZES[dt]), &scratch));
     g.scratch = scratch;
-    g.iscratch = ibytes ? (int64_t *)((char *)scratch + vbytes) : nullptr;
   }
   int *w = nullptr;
   pdlgb300_error e = status_word(&w);

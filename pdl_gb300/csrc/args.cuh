@@ -135,14 +135,12 @@ struct SortArgs {
   int bad;
   uint64_t abad, obad;
   int abad_isnan;
-  void *scratch;      // long rows: the merge sort's buffers (qsorti: rows x n private copies)
-  int64_t *iscratch;  // rows x n indices (qsorti)
+  void *scratch;      // long rows: the merge sort's buffers
   int *err;           // bit 0: a scan left its range (never expected)
 };
 pdlgb300_error launch_sortred(int kind, int dt, const SortArgs &g, cudaStream_t s);
-// scratch bytes of the merge sort of rows longer than SORT_SHARED_MAXN (all
-// kinds but qsorti, which keeps a private copy of each row: rows x n values)
-size_t sortred_long_scratch(int64_t rows, int64_t n, int tsize);
+// scratch bytes of the merge sort of rows longer than SORT_SHARED_MAXN
+size_t sortred_long_scratch(int kind, int64_t rows, int64_t n, int tsize);
 // rows up to this length sort in shared memory (warp or block kernels); the
 // scratch copies serve longer rows only
 constexpr int64_t SORT_SHARED_MAXN = 8192;

@@ -194,44 +194,6 @@ __device__ __forceinline__ void finish_values(const SortArgs &g, const T *tmp, i
   }
 }
 
-template <class T, int K, bool BAD>
-__global__ void __launch_bounds__(128) k_sortred(const SortArgs g) {
-  const Bad<T> bv{from_bits<T>(g.abad), (bool)g.abad_isnan};
-  const T obad = from_bits<T>(g.obad);
-  for (int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; row < g.rows;
-       row += (int64_t)gridDim.x * blockDim.x) {
-    int64_t offs[MAXP];
-    loop_offsets(g.L, row, offs);
-    const T *a = reinterpret_cast<const T *>(g.a) + offs[0];
-    T *tmp = reinterpret_cast<T *>(g.scratch) + row * g.n;
-    const int ob = g.out_pdl;
-    if constexpr (K == SR_QSORTI) {
-      int64_t *ix = g.iscratch + row * g.n;
-      int64_t *out = reinterpret_cast<int64_t *>(g.b) + offs[ob];
-      int64_t nn = 0, nb = g.n - 1;
-      for (int64_t t = 0; t < g.n; t++) {
-        const T v = a[t * g.inc_a];
-        tmp[t] = v;
-        if (BAD && bv.is(v)) ix[nb--] = t;
-        else ix[nn++] = t;
-      }
-      if (nn > 0 && !qs_indices<T, int64_t>(tmp, ix, 0, nn - 1)) atomicOr(g.err, 1);
-      for (int64_t t = 0; t < g.n; t++) out[t * g.inc_b] = ix[t];
-      continue;
-    }
-    // the good elements (all of them for modeover, which has no bad rule)
-    int64_t nn = 0;
-    for (int64_t t = 0; t < g.n; t++) {
-      const T v = a[t * g.inc_a];
-      if (K != SR_MODE && BAD && bv.is(v)) continue;
-      tmp[nn++] = v;
-    }
-    T *out = reinterpret_cast<T *>(g.b) + offs[ob];
-    if (nn > 0 && !qs_values<T>(tmp, 0, nn - 1)) atomicOr(g.err, 1);
-    finish_values<T, K>(g, tmp, nn, offs, out, obad, 0, 1);
-  }
-}
-
 // Short rows (n <= SF_MAX): one warp per row over shared memory.  Where
 // the result cannot depend on how the row is sorted -- the good values
 // hold no NaN and not both -0 and +0 (for qsorti also no two equal
@@ -625,9 +587,14 @@ __global__ void __launch_bounds__(LS_THREADS) k_lsort_tile(const SortArgs g, int
   }
 }
 
-template <class T>
+template <class T> struct LsLess {
+  __device__ bool operator()(const T &a, const T &b) const { return a < b; }
+};
+
+template <class T, class Less>
 __global__ void __launch_bounds__(LS_MT) k_lsort_merge(const T *in, T *out, int64_t np, int64_t w,
                                                        int64_t rows) {
+  const Less less;
   const int64_t per_row = np / LS_PER;
   for (int64_t q = (int64_t)blockIdx.x * LS_MT + threadIdx.x; q < rows * per_row;
        q += (int64_t)gridDim.x * LS_MT) {
@@ -640,14 +607,14 @@ __global__ void __launch_bounds__(LS_MT) k_lsort_merge(const T *in, T *out, int6
     int64_t lo = d - nb > 0 ? d - nb : 0, hi = d < na ? d : na;
     while (lo < hi) {  // A elements among the first d outputs
       const int64_t mid = (lo + hi) >> 1;
-      if (!(B[d - 1 - mid] < A[mid])) lo = mid + 1;
+      if (!less(B[d - 1 - mid], A[mid])) lo = mid + 1;
       else hi = mid;
     }
     int64_t i = lo, j = d - lo;
     T *dst = out + row * np + o;
 #pragma unroll
     for (int e = 0; e < LS_PER; e++) {
-      const bool takeA = j >= nb || (i < na && !(B[j] < A[i]));
+      const bool takeA = j >= nb || (i < na && !less(B[j], A[i]));
       dst[e] = takeA ? A[i++] : B[j++];
     }
   }
@@ -693,6 +660,180 @@ __global__ void __launch_bounds__(LS_FT) k_lsort_finish(const SortArgs g, const 
   }
 }
 
+// qsorti of rows longer than SB_MAX: (value, index) pairs.  Bad elements
+// and the padding past the row's end carry LS_PAD in the index and sort
+// after every good pair, by index.  Where the good values hold no NaN, not
+// both zeros and no two equal values, the quicksort's order of indices is
+// the sorted one; the bad indices follow in the order the reference leaves
+// them (filled from the row's end backwards).  Other rows: the reference's
+// quicksort on one thread, as before.
+constexpr int64_t LS_PAD = (int64_t)1 << 62;
+constexpr int LSI_TILE = 2048;  // pairs per tile: 32 KiB of shared memory
+
+template <class T> struct alignas(16) LsPair {
+  T v;
+  int64_t i;
+};
+template <class T> struct LsPairLess {
+  __device__ bool operator()(const LsPair<T> &a, const LsPair<T> &b) const {
+    const bool pa = (a.i & LS_PAD) != 0, pb = (b.i & LS_PAD) != 0;
+    if (pa != pb) return pb;
+    if (!pa) {
+      if (a.v < b.v) return true;
+      if (b.v < a.v) return false;
+    }
+    return a.i < b.i;
+  }
+};
+
+template <class T, bool BAD>
+__global__ void __launch_bounds__(LS_THREADS) k_lsorti_tile(const SortArgs g, int64_t np,
+                                                            LsPair<T> *buf,
+                                                            unsigned long long *cnt, int *flags) {
+  __shared__ LsPair<T> sv[LSI_TILE];
+  __shared__ int s_good, s_fl;
+  const LsPairLess<T> less;
+  const Bad<T> bv{from_bits<T>(g.abad), (bool)g.abad_isnan};
+  const int64_t tiles = np / LSI_TILE;
+  const int tid = threadIdx.x;
+  for (int64_t bt = blockIdx.x; bt < g.rows * tiles; bt += gridDim.x) {
+    const int64_t row = bt / tiles, t0 = (bt - row * tiles) * LSI_TILE;
+    int64_t offs[MAXP];
+    loop_offsets(g.L, row, offs);
+    const T *a = reinterpret_cast<const T *>(g.a) + offs[0];
+    if (tid == 0) {
+      s_good = 0;
+      s_fl = 0;
+    }
+    __syncthreads();
+    int good = 0, fl = 0;
+    for (int i = tid; i < LSI_TILE; i += LS_THREADS) {
+      const int64_t idx = t0 + i;
+      LsPair<T> p{(T)0, idx | LS_PAD};
+      if (idx < g.n) {
+        const T x = a[idx * g.inc_a];
+        p.v = x;
+        if (!(BAD && bv.is(x))) {
+          p.i = idx;
+          good++;
+          if constexpr (std::is_floating_point_v<T>) {
+            if (x != x) fl |= LS_NAN;
+            else if (x == (T)0) fl |= signbit(x) ? LS_NEG0 : LS_POS0;
+          }
+        }
+      }
+      sv[i] = p;
+    }
+    if (good) atomicAdd(&s_good, good);
+    if (fl) atomicOr(&s_fl, fl);
+    __syncthreads();
+    for (int k = 2; k <= LSI_TILE; k <<= 1) {
+      for (int j = k >> 1; j > 0; j >>= 1) {
+#pragma unroll
+        for (int q = 0; q < LSI_TILE / (2 * LS_THREADS); q++) {
+          const int pi = q * LS_THREADS + tid;
+          const int i = ((pi / j) * 2 * j) + (pi % j), ixj = i + j;
+          const bool up = (i & k) == 0;
+          const LsPair<T> x = sv[i], y = sv[ixj];
+          if (less(y, x) == up) {
+            sv[i] = y;
+            sv[ixj] = x;
+          }
+        }
+        __syncthreads();
+      }
+    }
+    LsPair<T> *o = buf + row * np + t0;
+    for (int i = tid; i < LSI_TILE; i += LS_THREADS) o[i] = sv[i];
+    if (tid == 0) {
+      if (s_good) atomicAdd(&cnt[row], (unsigned long long)s_good);
+      if (s_fl) atomicOr(&flags[row], s_fl);
+    }
+    __syncthreads();
+  }
+}
+
+template <class T, bool BAD>
+__global__ void __launch_bounds__(LS_FT) k_lsorti_finish(const SortArgs g, const LsPair<T> *sorted,
+                                                         LsPair<T> *spare, int64_t np,
+                                                         const unsigned long long *cnt,
+                                                         const int *flags) {
+  const Bad<T> bv{from_bits<T>(g.abad), (bool)g.abad_isnan};
+  for (int64_t row = blockIdx.x; row < g.rows; row += gridDim.x) {
+    int64_t offs[MAXP];
+    loop_offsets(g.L, row, offs);
+    int64_t *out = reinterpret_cast<int64_t *>(g.b) + offs[g.out_pdl];
+    const int fl = flags[row];
+    const int64_t nn = (int64_t)cnt[row];
+    const LsPair<T> *p = sorted + row * np;
+    bool unsafe = (fl & LS_NAN) || ((fl & LS_NEG0) && (fl & LS_POS0));
+    if (!unsafe) {  // equal good values: the quicksort's order of their indices is its own
+      int tie = 0;
+      for (int64_t k = threadIdx.x; k + 1 < nn; k += LS_FT)
+        if (!(p[k].v < p[k + 1].v)) tie = 1;
+      unsafe = __syncthreads_or(tie) != 0;
+    }
+    if (unsafe) {
+      if (threadIdx.x == 0) {
+        const T *a = reinterpret_cast<const T *>(g.a) + offs[0];
+        T *tmp = reinterpret_cast<T *>(spare + row * np);
+        int64_t *ix = reinterpret_cast<int64_t *>(spare + row * np) + g.n;
+        int64_t m = 0, nb = g.n - 1;
+        for (int64_t t = 0; t < g.n; t++) {
+          const T v = a[t * g.inc_a];
+          tmp[t] = v;
+          if (BAD && bv.is(v)) ix[nb--] = t;
+          else ix[m++] = t;
+        }
+        if (m > 0 && !qs_indices<T, int64_t>(tmp, ix, 0, m - 1)) atomicOr(g.err, 1);
+        for (int64_t t = 0; t < g.n; t++) out[t * g.inc_b] = ix[t];
+      }
+    } else {
+      const int64_t nbad = g.n - nn;
+      for (int64_t t = threadIdx.x; t < g.n; t += LS_FT)
+        out[t * g.inc_b] = t < nn ? p[t].i : (p[nn + (nbad - 1 - (t - nn))].i & ~LS_PAD);
+    }
+    __syncthreads();
+  }
+}
+
+int64_t lsorti_np(int64_t n) { return (n + LSI_TILE - 1) / LSI_TILE * LSI_TILE; }
+
+template <class T>
+pdlgb300_error go_lsorti(const SortArgs &g, cudaStream_t s) {
+  pdlgb300_error e = pgh::ok();
+  const int nsm = pgh::num_sms();
+  const int64_t np = lsorti_np(g.n), tiles = np / LSI_TILE;
+  using E = LsPair<T>;
+  E *b0 = reinterpret_cast<E *>(g.scratch);
+  E *b1 = b0 + g.rows * np;
+  unsigned long long *cnt = reinterpret_cast<unsigned long long *>(b1 + g.rows * np);
+  int *flags = reinterpret_cast<int *>(cnt + g.rows);
+  if (!pgh::cuda_check(cudaMemsetAsync(cnt, 0, (size_t)g.rows * (sizeof *cnt + sizeof *flags), s),
+                       &e, "lsorti counters"))
+    return e;
+  const int64_t gt = std::max<int64_t>(1, std::min<int64_t>(g.rows * tiles, (int64_t)nsm * 16));
+  if (g.bad) k_lsorti_tile<T, true><<<(int)gt, LS_THREADS, 0, s>>>(g, np, b0, cnt, flags);
+  else k_lsorti_tile<T, false><<<(int)gt, LS_THREADS, 0, s>>>(g, np, b0, cnt, flags);
+  if (!pgh::cuda_check(cudaGetLastError(), &e, "k_lsorti_tile")) return e;
+  pgh::record_kernel("k_lsorti_tile", gt, LS_THREADS);
+  E *cur = b0, *nxt = b1;
+  const int64_t gm = std::max<int64_t>(
+      1, std::min<int64_t>((g.rows * (np / LS_PER) + LS_MT - 1) / LS_MT, (int64_t)nsm * 32));
+  for (int64_t w = LSI_TILE; w < np; w *= 2) {
+    k_lsort_merge<E, LsPairLess<T>><<<(int)gm, LS_MT, 0, s>>>(cur, nxt, np, w, g.rows);
+    if (!pgh::cuda_check(cudaGetLastError(), &e, "k_lsort_merge")) return e;
+    pgh::record_kernel("k_lsort_merge", gm, LS_MT);
+    std::swap(cur, nxt);
+  }
+  const int64_t gf = std::max<int64_t>(1, std::min<int64_t>(g.rows, (int64_t)nsm * 16));
+  if (g.bad) k_lsorti_finish<T, true><<<(int)gf, LS_FT, 0, s>>>(g, cur, nxt, np, cnt, flags);
+  else k_lsorti_finish<T, false><<<(int)gf, LS_FT, 0, s>>>(g, cur, nxt, np, cnt, flags);
+  if (!pgh::cuda_check(cudaGetLastError(), &e, "k_lsorti_finish")) return e;
+  pgh::record_kernel("k_lsorti_finish", gf, LS_FT);
+  return e;
+}
+
 // scratch of the long-row merge sort: two buffers of rows x np values,
 // then the rows' good counts and flags
 int64_t lsort_np(int64_t n) { return (n + LS_TILE - 1) / LS_TILE * LS_TILE; }
@@ -718,7 +859,7 @@ pdlgb300_error go_lsort(const SortArgs &g, cudaStream_t s) {
   const int64_t gm = std::max<int64_t>(
       1, std::min<int64_t>((g.rows * (np / LS_PER) + LS_MT - 1) / LS_MT, (int64_t)nsm * 32));
   for (int64_t w = LS_TILE; w < np; w *= 2) {
-    k_lsort_merge<T><<<(int)gm, LS_MT, 0, s>>>(cur, nxt, np, w, g.rows);
+    k_lsort_merge<T, LsLess<T>><<<(int)gm, LS_MT, 0, s>>>(cur, nxt, np, w, g.rows);
     if (!pgh::cuda_check(cudaGetLastError(), &e, "k_lsort_merge")) return e;
     pgh::record_kernel("k_lsort_merge", gm, LS_MT);
     std::swap(cur, nxt);
@@ -767,13 +908,8 @@ pdlgb300_error go_sort(const SortArgs &g, cudaStream_t s) {
     return e;
   }
   if (!g.scratch) return pgh::err(PDLGB300_EFATAL, "sort: no scratch for long rows");
-  if constexpr (K != SR_QSORTI) return go_lsort<T, K>(g, s);
-  const int64_t grid = std::max<int64_t>(1, std::min<int64_t>((g.rows + 127) / 128, (int64_t)nsm * 16));
-  if (g.bad) k_sortred<T, K, true><<<(int)grid, 128, 0, s>>>(g);
-  else k_sortred<T, K, false><<<(int)grid, 128, 0, s>>>(g);
-  if (!pgh::cuda_check(cudaGetLastError(), &e, "k_sortred")) return e;
-  pgh::record_kernel("k_sortred", grid, 128);
-  return e;
+  if constexpr (K == SR_QSORTI) return go_lsorti<T>(g, s);
+  else return go_lsort<T, K>(g, s);
 }
 
 template <int DT>
@@ -795,8 +931,10 @@ pdlgb300_error sort_family(int k, const SortArgs &g, cudaStream_t s) {
 
 }  // namespace
 
-size_t sortred_long_scratch(int64_t rows, int64_t n, int tsize) {
-  return (size_t)2 * rows * lsort_np(n) * tsize + (size_t)rows * (sizeof(unsigned long long) + sizeof(int));
+size_t sortred_long_scratch(int kind, int64_t rows, int64_t n, int tsize) {
+  const size_t buf = kind == SR_QSORTI ? (size_t)2 * rows * lsorti_np(n) * 16
+                                       : (size_t)2 * rows * lsort_np(n) * tsize;
+  return buf + (size_t)rows * (sizeof(unsigned long long) + sizeof(int));
 }
 
 pdlgb300_error launch_sortred(int k, int dt, const SortArgs &g, cudaStream_t s) {

@@ -943,8 +943,8 @@ def test_sort_based_long_rows(gpu, op, t):
 
 
 @pytest.mark.parametrize("t", ["byte", "ushort", "long", "longlong", "float", "double"])
-@pytest.mark.parametrize("op", ["qsort", "medover", "oddmedover", "pctover", "oddpctover",
-                                "modeover"])
+@pytest.mark.parametrize("op", ["qsort", "qsorti", "medover", "oddmedover", "pctover",
+                                "oddpctover", "modeover"])
 def test_sort_based_rows_beyond_shared_memory(gpu, op, t):
     """Rows longer than 8192 values: a merge sort (tiles of 4096 sorted in
     shared memory, then merge passes) wherever the good values hold no NaN
@@ -975,8 +975,26 @@ def test_sort_based_rows_beyond_shared_memory(gpu, op, t):
         x = to_pdl(a, t, badflag=bf)
         ins = [x, P.pdl(np.array(0.37))] if op in ("pctover", "oddpctover") else [x]
         got, exp = _run_both(op, ins)
-        assert P.last_launch_info()["kernel"] == "k_lsort_finish"
+        assert P.last_launch_info()["kernel"] == ("k_lsorti_finish" if op == "qsorti"
+                                                  else "k_lsort_finish")
         _bits_equal(got, exp, f"{op} {t} {a.shape} bad={bf}")
+
+
+@pytest.mark.parametrize("t", ["float", "double", "long", "ulonglong"])
+def test_qsorti_long_rows_distinct_values(gpu, t):
+    """qsorti of rows longer than 8192 with all good values distinct: the
+    (value, index) merge sort gives the quicksort's order; bad indices
+    follow in the reference's order (from the row's end backwards)."""
+    rng = seeded(("lsorti", t))
+    n = (1 << 20) + 77
+    clean = np.stack([rng.permutation(n), rng.permutation(n)]).astype(NP_DTYPES[type_code(t)])
+    marked = clean.copy()
+    marked[rng.random(clean.shape) < 0.03] = P.default_badvalue(type_code(t))
+    for a, bf in ((clean, False), (marked, True)):
+        x = to_pdl(a, t, badflag=bf)
+        got, exp = _run_both("qsorti", [x])
+        assert P.last_launch_info()["kernel"] == "k_lsorti_finish"
+        _bits_equal(got, exp, f"qsorti {t} bad={bf}")
 
 
 @pytest.mark.parametrize("op", ["qsort", "medover", "pctover"])
@@ -1002,7 +1020,7 @@ def test_sort_beyond_shared_memory_edges(gpu, op):
 def test_row_block_scan_strided_rows(gpu):
     """The block-per-row scan over every other row of a matrix (a row
     increment of two rows), and into an output slice of a larger array."""
-    rng = seeded("rowblk-stride")
+    rng = seeded(("rowblk", "stride"))
     a, _ = rand_array(rng, "float", (7400, 16_400), -10, 10)
     x = to_pdl(a, "float").slice(slice(None), slice(0, None, 2))   # rows 0, 2, 4, ...
     got, exp = _run_both("cumusumover", [x])
