@@ -509,12 +509,12 @@ __global__ void __launch_bounds__(SB_THREADS) k_sortred_block(const SortArgs g) 
 //   puts a top value (above every good value) in place of bad elements and
 //   past the row's end, sorts the tile with a bitonic network in shared
 //   memory, and counts the row's good values and notes NaN and zero signs.
-// * k_lsort_merge: merge passes, runs of w -> 2w, each thread 16 outputs
+// * k_lsort_merge: merge passes, runs of w -> 2w, each thread 8 outputs
 //   found by a merge-path search (equal values: the first run's first).
 // * k_lsort_finish: the outputs from the sorted good prefix; a row with
 //   NaN or both zeros is sorted again by one thread with the reference's
 //   quicksort over its elements in their order, as k_sortred does.
-constexpr int LS_TILE = 4096, LS_THREADS = 512, LS_PER = 16, LS_MT = 256, LS_FT = 256;
+constexpr int LS_TILE = 4096, LS_THREADS = 512, LS_PER = 8, LS_MT = 256, LS_FT = 256;
 
 template <class T> __device__ __forceinline__ T ls_top() {
   if constexpr (std::is_floating_point_v<T>) return (T)INFINITY;
