@@ -348,18 +348,18 @@ __device__ __forceinline__ void split1(float x, __nv_bfloat16 (&h)[3]) {
 
 // Rows whose k is contiguous (s_k == 1): a thread splits 8 consecutive k of
 // one row and writes 16 bytes per limb; k past K (the padding) is zero.
+// Each thread takes two such items per round, both loads issued first.
 template <int LIMBS>
 __global__ void __launch_bounds__(256) k_split(const SplitArgs g) {
   const int64_t kc = g.Kp / 8, nrow = g.rows * g.nb, total = nrow * kc;
   const int64_t per_limb = g.nb * g.rows * g.Kp;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
-       i += (int64_t)gridDim.x * blockDim.x) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  auto load = [&](int64_t i, float (&x)[8]) {
     const int64_t rr = i / kc, k0 = (i - rr * kc) * 8;
     const int64_t z = rr / g.rows, r = rr - z * g.rows;
     int64_t offs[MAXP];
     loop_offsets(g.L, z, offs);
     const float *src = g.src + offs[g.p] + r * g.s_row;
-    float x[8];
     if (k0 + 8 <= g.K && ((uintptr_t)(src + k0) & 15) == 0) {
       const float4 u = __ldcs(reinterpret_cast<const float4 *>(src + k0));
       const float4 v = __ldcs(reinterpret_cast<const float4 *>(src + k0 + 4));
@@ -369,6 +369,9 @@ __global__ void __launch_bounds__(256) k_split(const SplitArgs g) {
 #pragma unroll
       for (int e = 0; e < 8; e++) x[e] = k0 + e < g.K ? src[k0 + e] : 0.f;
     }
+  };
+  auto store = [&](int64_t i, const float (&x)[8]) {
+    const int64_t rr = i / kc, k0 = (i - rr * kc) * 8;
     __align__(16) __nv_bfloat16 o[3][8];
 #pragma unroll
     for (int e = 0; e < 8; e++) {
@@ -381,6 +384,14 @@ __global__ void __launch_bounds__(256) k_split(const SplitArgs g) {
 #pragma unroll
     for (int l = 0; l < LIMBS; l++)
       *reinterpret_cast<uint4 *>(d + l * per_limb) = *reinterpret_cast<const uint4 *>(o[l]);
+  };
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += 2 * stride) {
+    const bool two = i + stride < total;
+    float x0[8], x1[8];
+    load(i, x0);
+    if (two) load(i + stride, x1);
+    store(i, x0);
+    if (two) store(i + stride, x1);
   }
 }
 
