@@ -1022,6 +1022,8 @@ def main():
                     help="time only the float64 family (--ops) and print its object")
     ap.add_argument("--mm-only", action="store_true",
                     help="time only the float32 matmult workload and print its object")
+    ap.add_argument("--inner-only", action="store_true",
+                    help="time only the inner leg and print its object")
     ap.add_argument("--c4-only", action="store_true",
                     help="time only the adjoint workload and print its object")
     ap.add_argument("--c2-only", action="store_true",
@@ -1038,7 +1040,7 @@ def main():
         print(json.dumps(run_reference(args, rank, world)))
         return 0
     if (args.expr_only or args.sort_only or args.family_only or args.c2_only or args.c4_only
-            or args.mm_only):
+            or args.mm_only or args.inner_only):
         import torch
         import pdl_gb300 as P
         stream = torch.cuda.current_stream()
@@ -1050,7 +1052,8 @@ def main():
             hbm, bf16, kind = peaks()
             print(json.dumps(bench_matmult(args, P, torch, stream, bf16, kind)))
             return 0
-        fn = bench_expr if args.expr_only else bench_sort if args.sort_only else run_family
+        fn = (bench_expr if args.expr_only else bench_sort if args.sort_only
+              else bench_inner if args.inner_only else run_family)
         print(json.dumps(fn(args, P, torch, stream, peaks()[0])))
         return 0
     if world > 1:

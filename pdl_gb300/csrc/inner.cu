@@ -67,13 +67,21 @@ __device__ __forceinline__ void block_products(const V16<T> (&xa)[U], const V16<
     ((p[J] = IA::prod(xa[J / VEC].e[J % VEC], xb[J / VEC].e[J % VEC])), ...);
 }
 
+// Each thread streams its own 16-byte vectors of a and b through a ring of
+// INNER_ST stages in shared memory (cp.async), INNER_U vectors of each per
+// stage: two stages stay in flight while the third is multiplied and
+// summed, without holding registers (the float64 products need them).  The
+// order of the products and sums is that of plain loads.
+constexpr int INNER_ST = 3, INNER_U = 4;
+constexpr int INNER_SLOT_B = INNER_ST * INNER_U * 2 * 16;  // ring bytes per thread
+
 template <class T, bool BAD>
 __global__ void __launch_bounds__(256) k_inner_rows(const InnerArgs g) {
   using IA = InnerAcc<T>;
   using A = typename IA::A;
   using P = typename IA::P;
   constexpr int VEC = 16 / sizeof(T);
-  constexpr int U = 4;  // 16-byte vectors of each operand in flight (8 for float64 cost 174 registers)
+  constexpr int U = INNER_U;
   Bad<T> ba{from_bits<T>(g.abad), (bool)g.abad_isnan};
   Bad<T> bb{from_bits<T>(g.bbad), (bool)g.bbad_isnan};
   const T cbad = from_bits<T>(g.cbad);
@@ -83,6 +91,12 @@ __global__ void __launch_bounds__(256) k_inner_rows(const InnerArgs g) {
   const int gid = G <= 32 ? (threadIdx.x >> 5) : 0;
   __shared__ A s_acc[32];
   __shared__ int s_bad[32];
+  extern __shared__ __align__(16) unsigned char inner_ring[];
+  // this thread's slots: [stage][operand][u], 16 bytes each, blockDim apart
+  const uint32_t ring0 = (uint32_t)__cvta_generic_to_shared(inner_ring) + threadIdx.x * 16u;
+  auto slot = [&](int st, int op, int u) {
+    return ring0 + (uint32_t)(((st * 2 + op) * U + u) * blockDim.x) * 16u;
+  };
   for (int64_t row = (int64_t)blockIdx.x * gpb + gid; row < g.rows;
        row += (int64_t)gridDim.x * gpb) {
     int64_t offs[MAXP];
@@ -96,19 +110,43 @@ __global__ void __launch_bounds__(256) k_inner_rows(const InnerArgs g) {
     int64_t nv = vec ? g.n / VEC : 0;
     const V16<T> *av = reinterpret_cast<const V16<T> *>(a);
     const V16<T> *bv = reinterpret_cast<const V16<T> *>(b);
-    for (int64_t k = lane; k < nv; k += (int64_t)G * U) {
+    const int64_t step = (int64_t)G * U;
+    auto issue = [&](int64_t k, int st) {
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        const int64_t kk = k + (int64_t)u * G;
+        if (kk < nv) {
+          asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(slot(st, 0, u)),
+                       "l"(av + kk)
+                       : "memory");
+          asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(slot(st, 1, u)),
+                       "l"(bv + kk)
+                       : "memory");
+        }
+      }
+      asm volatile("cp.async.commit_group;" ::: "memory");
+    };
+#pragma unroll
+    for (int st = 0; st < INNER_ST - 1; st++) issue(lane + st * step, st);
+    int st = 0;
+    for (int64_t k = lane; k < nv; k += step) {
+      asm volatile("cp.async.wait_group %0;" ::"n"(INNER_ST - 2) : "memory");
       V16<T> xa[U], xb[U];
       const bool full = k + (int64_t)(U - 1) * G < nv;
 #pragma unroll
       for (int u = 0; u < U; u++) {
-        int64_t kk = k + (int64_t)u * G;
-        if (full || kk < nv) {
-          float4 fa = __ldcs(reinterpret_cast<const float4 *>(av + kk));
-          float4 fb = __ldcs(reinterpret_cast<const float4 *>(bv + kk));
-          memcpy(&xa[u], &fa, 16);
-          memcpy(&xb[u], &fb, 16);
-        }
+        float4 fa, fb;
+        asm volatile("ld.shared.v4.f32 {%0,%1,%2,%3}, [%4];"
+                     : "=f"(fa.x), "=f"(fa.y), "=f"(fa.z), "=f"(fa.w)
+                     : "r"(slot(st, 0, u)));
+        asm volatile("ld.shared.v4.f32 {%0,%1,%2,%3}, [%4];"
+                     : "=f"(fb.x), "=f"(fb.y), "=f"(fb.z), "=f"(fb.w)
+                     : "r"(slot(st, 1, u)));
+        memcpy(&xa[u], &fa, 16);
+        memcpy(&xb[u], &fb, 16);
       }
+      // the stage read one iteration ago takes the next copies
+      issue(k + (INNER_ST - 1) * step, st == 0 ? INNER_ST - 1 : st - 1);
       if (full && !BAD) {
         P p[U * VEC];
         block_products<T, IA, U, VEC>(xa, xb, p, std::make_integer_sequence<int, U * VEC>{});
@@ -127,7 +165,9 @@ __global__ void __launch_bounds__(256) k_inner_rows(const InnerArgs g) {
           }
         }
       }
+      st = st == INNER_ST - 1 ? 0 : st + 1;
     }
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
     for (int64_t t = nv * VEC + lane; t < g.n; t += G) {
       T x = a[t * g.inc_a], y = b[t * g.inc_b];
       if (BAD && (ba.is(x) || bb.is(y))) anybad = 1;
@@ -207,11 +247,22 @@ pdlgb300_error inner_typed(const InnerArgs &g, cudaStream_t s) {
     pgh::record_kernel("k_inner_thread", grid, 128);
     return e;
   }
-  int block = g.group <= 32 ? 256 : g.group;
+  // a warp per row: blocks of 4 warps, so that four blocks' rings (48 KiB
+  // each) and registers fit on an SM
+  int block = g.group <= 32 ? 128 : g.group;
   int gpb = g.group <= 32 ? block / 32 : 1;
   int64_t grid = std::min<int64_t>((g.rows + gpb - 1) / gpb, (int64_t)1 << 30);
-  if (g.bad) k_inner_rows<T, true><<<(int)grid, block, 0, s>>>(g);
-  else k_inner_rows<T, false><<<(int)grid, block, 0, s>>>(g);
+  const size_t smem = (size_t)block * INNER_SLOT_B;
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_inner_rows<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         256 * INNER_SLOT_B);
+    cudaFuncSetAttribute(k_inner_rows<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         256 * INNER_SLOT_B);
+    attr = true;
+  }
+  if (g.bad) k_inner_rows<T, true><<<(int)grid, block, smem, s>>>(g);
+  else k_inner_rows<T, false><<<(int)grid, block, smem, s>>>(g);
   if (!pgh::cuda_check(cudaGetLastError(), &e, "k_inner_rows")) return e;
   pgh::record_kernel("k_inner_rows", grid, block);
   return e;
