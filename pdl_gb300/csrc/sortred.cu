@@ -199,7 +199,7 @@ __device__ __forceinline__ void finish_values(const SortArgs &g, const T *tmp, i
 // hold no NaN and not both -0 and +0 (for qsorti also no two equal
 // values) -- the warp sorts with a bitonic network (ties broken by
 // position, a total order); any other row is sorted by lane 0 with the
-// reference's quicksort over the same shared-memory copy, as in k_sortred.
+// reference's quicksort (qs_values / qs_indices) over the same copy.
 // The bad indices of qsorti are final when found: from the end backwards.
 constexpr int SF_MAX = 512, SF_WARPS = 4;
 
@@ -513,7 +513,7 @@ __global__ void __launch_bounds__(SB_THREADS) k_sortred_block(const SortArgs g) 
 //   found by a merge-path search (equal values: the first run's first).
 // * k_lsort_finish: the outputs from the sorted good prefix; a row with
 //   NaN or both zeros is sorted again by one thread with the reference's
-//   quicksort over its elements in their order, as k_sortred does.
+//   quicksort (qs_values) over its good elements in their order.
 constexpr int LS_TILE = 4096, LS_THREADS = 512, LS_PER = 8, LS_MT = 256, LS_FT = 256;
 
 template <class T> __device__ __forceinline__ T ls_top() {

@@ -920,7 +920,7 @@ def test_sort_based_empty_and_errors(gpu):
 @pytest.mark.parametrize("op", SORT_OPS + ["pctover", "modeover"])
 def test_sort_based_long_rows(gpu, op, t):
     """Rows of 513 to 8192 elements (a block per row in shared memory) and
-    beyond (the merge sort, or for qsorti one thread per row): ties, NaN and
+    beyond (the merge sort; for qsorti of (value, index) pairs): ties, NaN and
     signed zeros, distinct values (the network), bad values."""
     if op == "modeover" and t in ("float", "double"):
         return
