@@ -327,7 +327,28 @@ __global__ void __launch_bounds__(256, 3) k_expr_rows_vec(const ExprArgs g) {
       }
       V last;
       uint32_t lastm = 0;
-      for (int k = 0; k < nn; k++) {
+      // programs of one or two nodes without bad values: the node results
+      // stay in registers (node 0's operands are leaves, node 1's leaves or
+      // node 0)
+      bool done = false;
+      if constexpr (!BAD) {
+        if (nn <= 2) {
+          auto leaf_at = [&](int i) -> const V & {
+            return g.inc_n[i] != 0 ? stage[i * bd] : cslot[i * bd];
+          };
+          const ExprNode n0 = g.node[0];
+          apply_vec<T, VEC>(n0.op, leaf_at(n0.a), leaf_at(n0.b), last);
+          if (nn == 2) {
+            const ExprNode n1 = g.node[1];
+            const V r0 = last;
+            const V x = n1.a < EXPR_MAXL ? leaf_at(n1.a) : r0;
+            const V y = n1.b < EXPR_MAXL ? leaf_at(n1.b) : r0;
+            apply_vec<T, VEC>(n1.op, x, y, last);
+          }
+          done = true;
+        }
+      }
+      for (int k = 0; k < nn && !done; k++) {
         const ExprNode nd = g.node[k];
         // operand i: leaf i (ring slot of this stage, or its constant
         // slot) or node i - EXPR_MAXL
