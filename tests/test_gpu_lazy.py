@@ -144,3 +144,23 @@ def test_generic_kernel_matches_the_tiled_kernel(gpu):
     got, generic = got.numpy(), generic.numpy()
     assert np.array_equal(got, generic)
     assert np.array_equal(got, P.sumover(P.plus(P.mult(x, y), x)).numpy())
+
+
+@pytest.mark.parametrize("t", ["long", "float", "double"])
+def test_programs_of_one_to_eight_nodes(gpu, t):
+    """Programs of one or two nodes without bad values keep the node results
+    in registers, longer ones (and bad values) in shared-memory slots: one
+    to eight nodes over four leaves, node operands reaching back to every
+    earlier node, against the eager chain."""
+    rng = seeded(("nodes", t))
+    lv = [to_pdl(rand_array(rng, t, (6, 5000), -9, 9)[0], t) for _ in range(4)]
+    a, b, c, d = (P.lazy(x) for x in lv)
+    n0 = a * b
+    n1 = n0 + c
+    n2 = d - a
+    n3 = n1 * n2
+    progs = [a * b, (a - b) * (a - b), n0 + c * d, n3, n3 - n0, (n3 - n0) * n2,
+             ((n3 - n0) * n2) + n1, (((n3 - n0) * n2) + n1) - d]
+    for k, e in enumerate(progs):
+        for red in ("sumover", "minimum", "maximum_ind"):
+            _check(e, red, f"{t} program {k} {red}")
